@@ -1,0 +1,420 @@
+"""Benchmark of the GB300 SpGEMM engine (one JSON line on stdout).
+
+Default workload: the skewed square product C = A x A, A 1,048,576^2 CSR with
+lognormal row lengths (arithmetic mean 24, sigma 1.2, capped at 20,000), 70% of
+the columns within +-2,048 of the diagonal and 30% uniform, FP64 U[-1, 1),
+seeded synthetic data.  Metric: GFLOP/s = 2 x scalar products / time (the
+reference's definition, two_sided_spgemm.cpp:188-192).
+
+* value: device-resident operands, result left on the device; K timed steps
+  between CUDA events on the engine's stream (inputs exceed L2, no flush).
+* e2e: the same product through the C ABI with host (pinned) buffers: the
+  host->device copy of A and the device->host copy of C inside every step.
+* roofline: the numeric phase (K4, all bins), its algorithmic bytes over its
+  CUDA-event time measured in every timed step.
+* cpu_baseline: the reference's OpenMP row loop (the oracle port of
+  spgemm_exchange.cpp:258-325, or the reference's own build where it loads) on
+  a bounded slice of A's rows, timed on this host's cores.
+
+--impl reference runs only the CPU reference on the same workload and prints
+its own line.  With torchrun (N > 1) every rank runs an independent replica on
+its own GPU (the path's multi-GPU row sharding is not built); value sums the
+ranks' products over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "spgemm-hpc-thesis_gb300"))
+
+WORKLOADS = {
+    "powerlaw": "skewed C=A*A, A 1048576^2 lognormal rows (mean 24, sigma 1.2, cap 20000), "
+                "70% within +-2048 band, FP64 U[-1,1)",
+    "uniform": "C=A*B, A and B 65536^2, 16 distinct uniform columns per row, FP64 U[-1,1)",
+    "galerkin": "R*A then (R*A)*R^T, A 7-point Laplacian on 128^3, R 2x2x2 aggregation (262144 x 2097152)",
+}
+
+
+def make_workload(name: str):
+    """[(A, B)] host operands of the workload's products (chained products are
+    materialised once on the host)."""
+    import spgemm_gb300 as sg
+    if name == "powerlaw":
+        a = sg.synth_powerlaw(1 << 20, 24.0, 1.2, 20000, 2048, 0.7, seed=1)
+        return [(a, a)]
+    if name == "uniform":
+        return [(sg.synth_uniform(65536, 65536, 16, seed=1), sg.synth_uniform(65536, 65536, 16, seed=2))]
+    if name == "galerkin":
+        lap = sg.synth_laplacian3d(128)
+        r = sg.synth_restriction(128)
+        rt = sg.synth_restriction(128, transpose=True)
+        with sg.Engine(int(os.environ.get("LOCAL_RANK", "0"))) as eng:
+            ra = eng.multiply(r, lap)
+        return [(r, lap), (ra, rt)]
+    raise SystemExit(f"unknown workload {name}")
+
+
+def peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.gpu), "-lms", "100"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+            time.sleep(0.3)
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.15)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def all_max(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def all_sum(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# CPU reference (the oracle port, or the reference's own build where it loads)
+def cpu_reference():
+    from oracle import build as obuild
+    from oracle.oracle import Port, Reference
+    obuild.build_oracle()
+    if Reference.available():
+        try:
+            return Reference(), "reference"
+        except OSError:
+            pass
+    return Port(), "port"
+
+
+def row_slice(a, first: int, count: int):
+    import spgemm_gb300 as sg
+    rp = a.row_ptr[first:first + count + 1]
+    lo, hi = int(rp[0]), int(rp[-1])
+    return sg.Csr(count, a.cols, rp - lo, a.col[lo:hi], a.val[lo:hi])
+
+
+def time_cpu_slice(impl, kind: str, a, b, first: int, count: int, threads: int) -> tuple[float, int]:
+    """Seconds of one reference row-loop call on A[first:first+count] x B and its products."""
+    import spgemm_gb300 as sg
+    s = row_slice(a, first, count)
+    products = sg.scalar_products_host(s, b)
+    if kind == "reference":
+        secs, _ = impl.spgemm_timed(s, b, threads=threads, chunk=64, repeats=1)
+        return float(secs[0]), products
+    t0 = time.perf_counter()
+    impl.spgemm_omp_rows(s, b, 0, count, threads=threads, chunk=64)
+    return time.perf_counter() - t0, products
+
+
+def cpu_sample_rows(impl, kind, a, b, threads: int, target_s: float) -> tuple[int, int]:
+    """A centred row slice sized to take about target_s seconds."""
+    m = a.rows
+    n = min(m, 2048)
+    first = max(0, m // 2 - n // 2)
+    t, _ = time_cpu_slice(impl, kind, a, b, first, n, threads)
+    n = int(min(m, max(n, n * target_s / max(t, 1e-6))))
+    first = max(0, m // 2 - n // 2)
+    return first, n
+
+
+def run_reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    pairs = make_workload(args.workload)
+    impl, kind = cpu_reference()
+    threads = os.cpu_count() or 1
+    per_step = max(1.0, args.reference_step_seconds)
+    a, b = pairs[0]
+    first, n = cpu_sample_rows(impl, kind, a, b, threads, per_step)
+    for _ in range(args.warmup):
+        time_cpu_slice(impl, kind, a, b, first, n, threads)
+    tot_t, tot_p = 0.0, 0
+    for _ in range(args.steps):
+        t, p = time_cpu_slice(impl, kind, a, b, first, n, threads)
+        tot_t += t
+        tot_p += p
+    value = 2.0 * tot_p / tot_t / 1e9
+    sample = f"rows [{first}, {first + n}) of A ({n} of {a.rows} rows) x B, first product of the workload"
+    line = {
+        "impl": "reference", "metric": "GFLOP/s", "value": value, "unit": "GFLOP/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOADS[args.workload], "name": args.workload},
+        "cpu_baseline": {"value": value, "unit": "GFLOP/s", "cores": threads, "kind": kind, "sample": sample},
+        "e2e": {"value": value, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
+def run_gpu_arm(args, rank, world, local):
+    import torch
+    import spgemm_gb300 as sg
+    torch.cuda.set_device(local)
+    pairs = make_workload(args.workload)
+    eng = sg.Engine(local)
+    dev_pairs = []
+    for a, b in pairs:
+        da = a.to_device(local)
+        db = da if b is a else b.to_device(local)
+        dev_pairs.append((da, db))
+    products = sum(sg.scalar_products_host(a, b) for a, b in pairs)
+
+    # one untimed product per pair to learn nnz(C) (for the byte count and D2H size)
+    c_nnz = []
+    for da, db in dev_pairs:
+        r = eng.multiply(da, db, out="device")
+        c_nnz.append(r.nnz)
+        r.free()
+    bytes_alg = sum(sg.algorithmic_bytes(a, b, sg.scalar_products_host(a, b), n)
+                    for (a, b), n in zip(pairs, c_nnz))
+
+    stream = torch.cuda.ExternalStream(eng.stream, device=torch.device("cuda", local))
+
+    def step():
+        launches = 0
+        numeric_ms = 0.0
+        for da, db in dev_pairs:
+            r = eng.multiply(da, db, out="device")
+            t = eng.last_timings()
+            launches += t["launches"]
+            numeric_ms += t["ms_numeric"]
+            r.free()
+        return launches, numeric_ms
+
+    for _ in range(args.warmup):
+        step()
+    barrier(world)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches = 0
+    numeric_ms = 0.0
+    with ClockSampler(local) as clocks:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            l, nm = step()
+            launches += l
+            numeric_ms += nm
+        ev1.record(stream)
+        ev1.synchronize()
+    torch.cuda.synchronize()
+    barrier(world)
+    t_ms = ev0.elapsed_time(ev1)
+    t_max = all_max(t_ms, world)
+    total_products = all_sum(products * args.steps, world)
+    value = 2.0 * total_products / (t_max / 1e3) / 1e9
+
+    # e2e: host (pinned) operands in, host (pinned) result out, through the C ABI
+    e2e = None
+    if not args.no_e2e:
+        host_pairs = []
+        for a, b in pairs:
+            pa = _pinned_csr(a)
+            pb = pa if b is a else _pinned_csr(b)
+            host_pairs.append((pa, pb))
+        outs = [(_pinned_like(a.rows + 1, torch.int64), _pinned_like(n, torch.int32), _pinned_like(n, torch.float64))
+                for (a, _), n in zip(pairs, c_nnz)]
+        h2d = sum(_csr_bytes(a) + (0 if b is a else _csr_bytes(b)) for a, b in pairs)
+        d2h = sum(8 * (a.rows + 1) + 12 * n for (a, _), n in zip(pairs, c_nnz))
+
+        def e2e_step():
+            for (pa, pb), (orp, oci, ova) in zip(host_pairs, outs):
+                r = eng.multiply(pa, pb, out="device")
+                r._engine._check(sg.library().spg_result_download(
+                    eng.h, sg.C.byref(r._res), sg.C.c_void_p(orp.data_ptr()), sg.C.c_void_p(oci.data_ptr()),
+                    sg.C.c_void_p(ova.data_ptr())))
+                r.free()
+            return float(ova[0].item()) if ova.numel() else 0.0
+
+        for _ in range(max(1, args.warmup)):
+            e2e_step()
+        ke = max(1, min(args.steps, args.e2e_steps))
+        barrier(world)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            e2e_step()
+        torch.cuda.synchronize()
+        te = all_max(time.perf_counter() - t0, world)
+        e2e = {"value": 2.0 * all_sum(products * ke, world) / te / 1e9, "unit": "GFLOP/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": ke}
+
+    pk = peaks()
+    numeric_avg_s = numeric_ms / args.steps / 1e3
+    achieved = bytes_alg / numeric_avg_s / 1e9 if numeric_avg_s > 0 else None
+    traffic = None
+    tf = ROOT / "profiles" / f"traffic_{args.workload}.json"
+    if tf.exists():
+        traffic = json.loads(tf.read_text()).get("dram_bytes_per_step")
+    roofline = {"bound": "hbm", "kernel": "K4 numeric phase (all bins, one step)", "achieved": achieved,
+                "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": (achieved / pk["hbm_gbs"]) if achieved else None,
+                "peak_source": pk["source"], "traffic": traffic, "bytes_alg": int(bytes_alg),
+                "pipeline_frac": bytes_alg / (t_ms / args.steps / 1e3) / 1e9 / pk["hbm_gbs"]}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        impl, kind = cpu_reference()
+        threads = os.cpu_count() or 1
+        a, b = pairs[0]
+        first, n = cpu_sample_rows(impl, kind, a, b, threads, args.cpu_seconds)
+        t, p = time_cpu_slice(impl, kind, a, b, first, n, threads)
+        cpu = {"value": 2.0 * p / t / 1e9, "unit": "GFLOP/s", "cores": threads, "kind": kind,
+               "sample": f"rows [{first}, {first + n}) of A x B ({n} of {a.rows} rows, {p} products, {t:.2f} s)"}
+
+    if rank == 0:
+        line = {
+            "metric": "GFLOP/s", "value": value, "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOADS[args.workload], "name": args.workload,
+                       "products_per_step": int(products), "c_nnz": int(sum(c_nnz)),
+                       "l2": "inputs larger than L2 (no flush)" if args.workload == "powerlaw" else
+                             "inputs smaller than L2 (B stays resident between steps)",
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": int(launches), "clocks": clocks.summary(),
+            "phases_ms_last_step": {k: v for k, v in eng.last_timings().items()
+                                    if k.startswith("ms_")},
+        }
+        print(json.dumps(line))
+    eng.close()
+
+
+def _pinned_like(n, dtype):
+    import torch
+    return torch.empty(max(int(n), 1), dtype=dtype, pin_memory=True)
+
+
+def _pinned_csr(a):
+    import torch
+    import spgemm_gb300 as sg
+    rp = torch.from_numpy(a.row_ptr).pin_memory()
+    ci = torch.from_numpy(a.col).pin_memory()
+    va = torch.from_numpy(a.val).pin_memory()
+    m = sg.Csr(a.rows, a.cols, rp.numpy(), ci.numpy(), va.numpy())
+    m._keep = (rp, ci, va)
+    return m
+
+
+def _csr_bytes(a) -> int:
+    return 8 * (a.rows + 1) + 12 * a.nnz
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="powerlaw")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--reference-step-seconds", type=float, default=8.0)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, world, local = dist_init()
+    if args.impl == "reference":
+        run_reference_arm(args, rank, world)
+    else:
+        run_gpu_arm(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

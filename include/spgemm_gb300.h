@@ -1,0 +1,160 @@
+/* GB300-native SpGEMM engine: C ABI (libspgemm_gb300.so).
+ *
+ * The engine replaces the local CSR x CSR multiply of malchioman/SpGEMM-hpc-thesis
+ * on one GPU.  Matrices use the reference's CsrMatrix layout
+ * (src/common/csr_matrix.hpp:43-49): int32 rows/cols, int64 row offsets
+ * (rows+1 entries, first 0, last nnz), int32 column indices and FP64 values.
+ * Results follow the reference's output contract: every row sorted by column
+ * without duplicates, exact +0.0/-0.0 sums dropped, NaN and infinities kept,
+ * C.rows = A.rows, C.cols = B.cols.  Every stored value is the sequential FP64
+ * sum of its products in the reference's order (A entries, then B entries, in
+ * stored order; one rounding per multiply and per add), so results are
+ * bit-identical to the reference's serialSpgemm and spgemm().
+ *
+ * Threading: a handle owns one CUDA stream and its workspace; calls on one
+ * handle must not overlap.  Use one handle per host thread.
+ *
+ * Errors: every call returns an spg_status; spg_last_error(handle) gives the
+ * message of the last failure on that handle.  include/spgemm_gb300.hpp maps
+ * statuses back to the reference's exception types.
+ */
+#ifndef SPGEMM_GB300_H
+#define SPGEMM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    SPG_OK = 0,
+    SPG_INVALID_ARGUMENT = 1,      /* shapes, malformed CSR, B column outside B.cols (std::invalid_argument) */
+    SPG_OVERFLOW = 2,              /* a count beyond the engine's int64/int32 limits (std::overflow_error) */
+    SPG_OUT_OF_RANGE_COLUMN = 3,   /* an A column outside B's rows (std::runtime_error in the reference) */
+    SPG_OUT_OF_MEMORY = 4,         /* device allocation failed */
+    SPG_BUDGET_EXCEEDED = 5,       /* the request's footprint exceeds the handle's HBM budget */
+    SPG_DEVICE_TIMEOUT = 6,        /* a bounded wait ran out (serving loop) */
+    SPG_CUDA_ERROR = 7,            /* any other CUDA failure */
+    SPG_NOT_READY = 8,             /* spg_poll: the request has not finished */
+    SPG_CANCELLED = 9              /* spg_poll: the request was cancelled */
+} spg_status;
+
+typedef enum { SPG_HOST = 0, SPG_DEVICE = 1 } spg_location;
+
+/* Read-only CSR operand.  `location` says where the three arrays live; host
+ * arrays may be pageable or pinned (pinned copies are faster). */
+typedef struct {
+    int32_t rows, cols;
+    int64_t nnz;
+    const int64_t* row_ptr;
+    const int32_t* col;
+    const double* val;
+    int32_t location;  /* spg_location */
+} spg_csr_view;
+
+/* Result CSR.  The arrays are owned by the library (device memory for
+ * SPG_DEVICE results, malloc'd host memory for SPG_HOST results) and are
+ * released with spg_result_free. */
+typedef struct {
+    int32_t rows, cols;
+    int64_t nnz;
+    int64_t* row_ptr;
+    int32_t* col;
+    double* val;
+    int32_t location;
+    int32_t reserved;
+    int64_t products;  /* scalar products of this result (FLOP count = 2 * products) */
+} spg_csr_result;
+
+typedef struct {
+    int32_t device;             /* CUDA device ordinal */
+    int32_t reserved;
+    uint64_t hbm_budget_bytes;  /* largest device footprint a request may reserve; 0 = no limit */
+} spg_config;
+
+/* Per-phase device times of the last multiply on a handle (CUDA events). */
+typedef struct {
+    float ms_rowwork, ms_symbolic, ms_scan, ms_numeric, ms_compact, ms_total;
+    int64_t products, nnz, rows;
+    int64_t bin_rows[11];
+    int64_t launches;  /* kernels this library launched for the call */
+} spg_timings;
+
+typedef struct spg_handle spg_handle;
+
+/* ---- handle ----------------------------------------------------------- */
+spg_status spg_config_default(spg_config* config);
+spg_status spg_create(const spg_config* config, spg_handle** handle);
+void spg_destroy(spg_handle* handle);
+const char* spg_last_error(const spg_handle* handle);
+const char* spg_status_string(spg_status status);
+/* The handle's CUDA stream (a cudaStream_t) for callers that order their own work. */
+void* spg_stream(spg_handle* handle);
+
+/* ---- plain product ------------------------------------------------------
+ * C = A * B.  Replaces the local multiply
+ *   CsrMatrix spgemm(const CsrMatrix& localMatrixA, RowBlock localBBlock,
+ *                    const CsrMatrix& localMatrixB, const RemoteSparseRows&, MPI_Comm)
+ *   (src/baselines/spgemm_exchange.hpp:37-39; body spgemm_exchange.cpp:258-325)
+ * with B entirely local (localBBlock = {0, B.rows}, no halo rows), and its
+ * serial twin CsrMatrix serialSpgemm(const CsrMatrix&, const CsrMatrix&)
+ *   (src/common/spgemm_common.hpp:80; spgemm_common.cpp:131-178,470-472).
+ * Errors: A.cols != B.rows -> SPG_INVALID_ARGUMENT (spgemm_common.cpp:106-110);
+ * an A column outside [0, B.rows) -> SPG_OUT_OF_RANGE_COLUMN
+ * (spgemm_common.cpp:141-143; the baseline aborts through fail(),
+ * spgemm_exchange.cpp:82-85).  `out_location` selects where C is returned. */
+spg_status spg_multiply(spg_handle* handle, const spg_csr_view* A, const spg_csr_view* B, int32_t out_location,
+                        spg_csr_result* C);
+
+/* Copies a device result into caller host buffers of exactly C->rows+1 /
+ * C->nnz / C->nnz elements (any of them may be NULL to skip that array). */
+spg_status spg_result_download(spg_handle* handle, const spg_csr_result* C, int64_t* row_ptr, int32_t* col,
+                               double* val);
+spg_status spg_result_free(spg_handle* handle, spg_csr_result* C);
+
+/* Scalar products P = sum over A entries of nnz(B row); the reference's FLOP
+ * count is 2P.  Replaces std::int64_t scalarMultiplicationCount(const CsrMatrix&,
+ * const CsrMatrix&) (src/common/spgemm_common.hpp:81; spgemm_common.cpp:474-487),
+ * with the same errors as spg_multiply. */
+spg_status spg_scalar_multiplication_count(spg_handle* handle, const spg_csr_view* A, const spg_csr_view* B,
+                                           int64_t* products);
+
+/* Per-phase timings of the last spg_multiply / spg_accum_add on the handle. */
+spg_status spg_last_timings(const spg_handle* handle, spg_timings* timings);
+
+/* ---- accumulate mode -----------------------------------------------------
+ * Replaces trident::LocalAccumulator (src/trident/common/matrix_blocks.hpp:23-32;
+ * matrix_blocks.cpp:152-200): begin(rows, cols) <-> the constructor,
+ * add(A, B) <-> addProduct (C += A*B, products added after the values already
+ * held, each coordinate in order), finish <-> finish().  Shape mismatch
+ * (A.rows != rows, B.cols != cols or A.cols != B.rows) -> SPG_INVALID_ARGUMENT
+ * (matrix_blocks.cpp:155-157).  Exact zeros are absent from the result;
+ * dropping them between stages does not change any result, because a later
+ * stage's sum starting from +0.0 or from nothing is the same value.  One
+ * accumulation per handle at a time. */
+spg_status spg_accum_begin(spg_handle* handle, int32_t rows, int32_t cols);
+spg_status spg_accum_add(spg_handle* handle, const spg_csr_view* A, const spg_csr_view* B);
+spg_status spg_accum_finish(spg_handle* handle, int32_t out_location, spg_csr_result* C);
+
+/* ---- batched products ------------------------------------------------------
+ * n independent products C[i] = A[i] * B[i] in one set of launches per phase
+ * (one persistent launch per bin and phase over the concatenated rows of all
+ * products).  No reference counterpart: the reference multiplies one product
+ * per call (the loop of spgemm() calls in two_sided_spgemm.cpp:146-167).
+ * Per-product results and errors are those of spg_multiply; the first failing
+ * product's status is returned and no result is produced. */
+spg_status spg_multiply_batch(spg_handle* handle, int32_t n, const spg_csr_view* A, const spg_csr_view* B,
+                              int32_t out_location, spg_csr_result* C);
+
+/* ---- host staging helpers ------------------------------------------------- */
+/* Page-locked host memory (fast host<->device copies); free with spg_host_free. */
+void* spg_host_alloc(size_t bytes);
+void spg_host_free(void* ptr);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPGEMM_GB300_H */

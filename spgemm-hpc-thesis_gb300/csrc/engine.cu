@@ -1,0 +1,701 @@
+// Host side of the GB300 SpGEMM engine and its C ABI (include/spgemm_gb300.h).
+//
+// One call runs the phases on the handle's stream:
+//   stage operands -> K1 row work + bins -> [sync: bin sizes, errors]
+//   -> K2 symbolic per bin -> K3 scan -> [sync: C size] -> allocate C
+//   -> K4 numeric per bin -> [sync: stored count, errors]
+//   -> (K5 compaction only if some sum was an exact zero) -> result.
+// All rows of all products of a call are flattened into one set of bin lists,
+// so a batch of products costs the same number of launches as one product.
+// Device memory comes from the device's stream-ordered pool (cudaMallocAsync),
+// whose release threshold is raised so that repeated calls reuse memory.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/spgemm_gb300.h"
+#include "spg_common.cuh"
+
+
+using namespace spg;
+
+struct spg_handle {
+    int device = 0;
+    int num_sms = 152;
+    cudaStream_t stream = nullptr;
+    spg_config cfg{};
+    std::string err;
+    cudaEvent_t ev[6] = {};
+    spg_timings last{};
+    // accumulate mode: the running sum S (device result) and its shape
+    bool acc_active = false;
+    int32_t acc_rows = 0, acc_cols = 0;
+    spg_csr_result acc{};
+    bool acc_has = false;
+    // pinned control block for small device->host reads
+    void* ctrl = nullptr;
+};
+
+namespace {
+
+constexpr size_t kCtrlBytes = 4096;
+
+struct Failure {
+    spg_status status;
+    std::string message;
+};
+
+spg_status fail(spg_handle* h, spg_status s, const std::string& msg) {
+    if (h) h->err = msg;
+    return s;
+}
+
+void check_cuda(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return;
+    const spg_status s = (e == cudaErrorMemoryAllocation) ? SPG_OUT_OF_MEMORY : SPG_CUDA_ERROR;
+    throw Failure{s, std::string(what) + ": " + cudaGetErrorString(e)};
+}
+
+// Device allocations of one call; freed on the stream unless released to a result.
+class Arena {
+public:
+    explicit Arena(spg_handle* h) : h_(h) {}
+    ~Arena() {
+        for (void* p : live_)
+            if (p) cudaFreeAsync(p, h_->stream);
+    }
+    template <typename T>
+    T* alloc(size_t count, const char* what) {
+        void* p = nullptr;
+        check_cuda(cudaMallocAsync(&p, std::max<size_t>(count * sizeof(T), 16), h_->stream), what);
+        live_.push_back(p);
+        bytes_ += count * sizeof(T);
+        return static_cast<T*>(p);
+    }
+    void release(void* p) {
+        for (auto& q : live_)
+            if (q == p) q = nullptr;
+    }
+    void free_now(void* p) {
+        for (auto& q : live_)
+            if (q == p) {
+                cudaFreeAsync(q, h_->stream);
+                q = nullptr;
+            }
+    }
+    size_t bytes() const { return bytes_; }
+
+private:
+    spg_handle* h_;
+    std::vector<void*> live_;
+    size_t bytes_ = 0;
+};
+
+void sync(spg_handle* h) { check_cuda(cudaStreamSynchronize(h->stream), "cudaStreamSynchronize"); }
+
+void require(bool ok, spg_status s, const std::string& msg) {
+    if (!ok) throw Failure{s, msg};
+}
+
+// Checks what can be checked on the host without reading device memory.
+void check_view(const spg_csr_view* m, const char* name) {
+    require(m != nullptr, SPG_INVALID_ARGUMENT, std::string(name) + " is NULL");
+    require(m->rows >= 0 && m->cols >= 0 && m->nnz >= 0, SPG_INVALID_ARGUMENT,
+            std::string(name) + ": negative dimension or nnz");
+    require(m->row_ptr != nullptr, SPG_INVALID_ARGUMENT, std::string(name) + ": row_ptr is NULL");
+    require(m->nnz == 0 || (m->col && m->val), SPG_INVALID_ARGUMENT, std::string(name) + ": col/val is NULL");
+    require(m->location == SPG_HOST || m->location == SPG_DEVICE, SPG_INVALID_ARGUMENT,
+            std::string(name) + ": bad location");
+    if (m->location == SPG_HOST) {
+        require(m->row_ptr[0] == 0 && m->row_ptr[m->rows] == m->nnz, SPG_INVALID_ARGUMENT,
+                std::string(name) + ": row_ptr must start at 0 and end at nnz");
+    }
+}
+
+// A device view of an operand, copying host arrays in.
+CsrView stage(spg_handle* h, Arena& ar, const spg_csr_view* m) {
+    CsrView v;
+    v.rows = m->rows;
+    v.cols = m->cols;
+    v.nnz = m->nnz;
+    if (m->location == SPG_DEVICE) {
+        v.rp = m->row_ptr;
+        v.ci = m->col;
+        v.v = m->val;
+        return v;
+    }
+    int64_t* rp = ar.alloc<int64_t>(static_cast<size_t>(m->rows) + 1, "stage row_ptr");
+    int32_t* ci = ar.alloc<int32_t>(static_cast<size_t>(m->nnz), "stage col");
+    double* va = ar.alloc<double>(static_cast<size_t>(m->nnz), "stage val");
+    check_cuda(cudaMemcpyAsync(rp, m->row_ptr, sizeof(int64_t) * (static_cast<size_t>(m->rows) + 1),
+                               cudaMemcpyHostToDevice, h->stream), "H2D row_ptr");
+    if (m->nnz) {
+        check_cuda(cudaMemcpyAsync(ci, m->col, sizeof(int32_t) * m->nnz, cudaMemcpyHostToDevice, h->stream), "H2D col");
+        check_cuda(cudaMemcpyAsync(va, m->val, sizeof(double) * m->nnz, cudaMemcpyHostToDevice, h->stream), "H2D val");
+    }
+    v.rp = rp;
+    v.ci = ci;
+    v.v = va;
+    return v;
+}
+
+struct JobIn {
+    const spg_csr_view* A;
+    const spg_csr_view* B;
+    CsrView S;  // S.rp == nullptr: none
+};
+
+struct DevResult {
+    int32_t rows = 0, cols = 0;
+    int64_t nnz = 0, products = 0;
+    int64_t* rp = nullptr;
+    int32_t* ci = nullptr;
+    double* v = nullptr;
+};
+
+struct Ctrl {  // layout of the pinned control block and its device twin
+    Stats stats;
+    ErrWord err;
+    int64_t bin_off[kNumBins + 1];
+    unsigned long long cursor[kNumBins];
+    int64_t totals[2];  // scanned totals (symbolic, numeric)
+};
+
+spg_status map_err(const ErrWord& e, std::string& msg) {
+    char buf[160];
+    switch (e.code) {
+        case kErrColumnRange:
+            std::snprintf(buf, sizeof buf, "A contains a column index outside B's row range (A entry %lld)",
+                          static_cast<long long>(e.detail));
+            msg = buf;
+            return SPG_OUT_OF_RANGE_COLUMN;
+        case kErrOverflow:
+            std::snprintf(buf, sizeof buf, "count overflow (detail %lld)", static_cast<long long>(e.detail));
+            msg = buf;
+            return SPG_OVERFLOW;
+        default:
+            std::snprintf(buf, sizeof buf, "malformed CSR input (check %d, detail %lld)", e.where,
+                          static_cast<long long>(e.detail));
+            msg = buf;
+            return SPG_INVALID_ARGUMENT;
+    }
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+}
+
+// The phase pipeline for one or more products.  Results stay on the device.
+void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevResult>& out, bool count_only,
+                  int64_t* products_out) {
+    cudaStream_t st = h->stream;
+    Arena ar(h);
+    const int njobs = static_cast<int>(in.size());
+    std::vector<Job> jobs(njobs);
+    std::vector<int64_t> row_base(njobs + 1, 0);
+    for (int j = 0; j < njobs; ++j) {
+        check_view(in[j].A, "A");
+        check_view(in[j].B, "B");
+        require(in[j].A->cols == in[j].B->rows, SPG_INVALID_ARGUMENT, "SpGEMM requires A.cols == B.rows");
+        row_base[j + 1] = row_base[j] + in[j].A->rows;
+    }
+    const int64_t total_rows = row_base[njobs];
+    for (int j = 0; j < njobs; ++j) {
+        const spg_csr_view* a = in[j].A;
+        const spg_csr_view* b = in[j].B;
+        jobs[j].A = stage(h, ar, a);
+        // C = A*A from one host matrix: copy it to the device once
+        const bool same = a->location == b->location && a->row_ptr == b->row_ptr && a->col == b->col &&
+                          a->val == b->val && a->rows == b->rows && a->cols == b->cols && a->nnz == b->nnz;
+        jobs[j].B = same ? jobs[j].A : stage(h, ar, b);
+        jobs[j].S = in[j].S;
+        jobs[j].row_base = row_base[j];
+    }
+    // per-row workspace: ub (rows), cnt and nz (rows + 1 per job)
+    const size_t slots = static_cast<size_t>(total_rows + njobs);
+    int64_t* ub = ar.alloc<int64_t>(static_cast<size_t>(total_rows), "ub");
+    int64_t* cnt = ar.alloc<int64_t>(slots, "cnt");
+    int64_t* nz = ar.alloc<int64_t>(slots, "nz");
+    int64_t* items = ar.alloc<int64_t>(static_cast<size_t>(total_rows), "items");
+    int64_t* d_row_base = ar.alloc<int64_t>(static_cast<size_t>(njobs) + 1, "row_base");
+    Ctrl* d_ctrl = ar.alloc<Ctrl>(1, "ctrl");
+    Job* d_jobs = ar.alloc<Job>(static_cast<size_t>(njobs), "jobs");
+    for (int j = 0; j < njobs; ++j) {
+        jobs[j].ub = ub + row_base[j];
+        jobs[j].cnt = cnt + row_base[j] + j;
+        jobs[j].nz = nz + row_base[j] + j;
+    }
+    check_cuda(cudaMemsetAsync(cnt, 0, slots * sizeof(int64_t), st), "memset cnt");
+    check_cuda(cudaMemsetAsync(nz, 0, slots * sizeof(int64_t), st), "memset nz");
+    check_cuda(cudaMemsetAsync(d_ctrl, 0, sizeof(Ctrl), st), "memset ctrl");
+    check_cuda(cudaMemcpyAsync(d_row_base, row_base.data(), sizeof(int64_t) * (njobs + 1), cudaMemcpyHostToDevice, st),
+               "H2D row_base");
+    check_cuda(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(Job) * njobs, cudaMemcpyHostToDevice, st), "H2D jobs");
+
+    Ctrl* hc = static_cast<Ctrl*>(h->ctrl);
+    int64_t launches = total_rows > 0 ? 3 : 1;
+    cudaEventRecord(h->ev[0], st);
+    launch_rowwork(d_jobs, njobs, d_row_base, total_rows, &d_ctrl->stats, &d_ctrl->err, st);
+    launch_bin_offsets(&d_ctrl->stats, d_ctrl->bin_off, st);
+    launch_bin_scatter(d_jobs, njobs, d_row_base, total_rows, d_ctrl->bin_off, d_ctrl->cursor, items, st);
+    check_cuda(cudaGetLastError(), "K1 launch");
+    cudaEventRecord(h->ev[1], st);
+    check_cuda(cudaMemcpyAsync(hc, d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, st), "D2H ctrl");
+    sync(h);  // sync 1: bins and input checks
+    if (hc->err.code) {
+        std::string msg;
+        const spg_status s = map_err(hc->err, msg);
+        throw Failure{s, msg};
+    }
+    const int64_t products = static_cast<int64_t>(hc->stats.products);
+    const int64_t max_ub = static_cast<int64_t>(hc->stats.max_ub);
+    if (products_out) *products_out = products;
+    if (count_only) {
+        h->last = spg_timings{};
+        h->last.products = products;
+        h->last.launches = launches;
+        return;
+    }
+    require(max_ub < (int64_t{1} << 30), SPG_OVERFLOW,
+            "an output row has more than 2^30 scalar products (engine limit)");
+    int64_t bin_count[kNumBins], bin_off[kNumBins + 1];
+    for (int b = 0; b < kNumBins; ++b) bin_count[b] = static_cast<int64_t>(hc->stats.bin_count[b]);
+    for (int b = 0; b <= kNumBins; ++b) bin_off[b] = hc->bin_off[b];
+
+    // heavy-row scratch shared by the symbolic and numeric phases
+    const int64_t heavy = bin_count[kBinHeavy];
+    size_t scratch_bytes = std::max(symbolic_scratch_bytes(kBinHeavy, max_ub, heavy, h->num_sms),
+                                    numeric_scratch_bytes(kBinHeavy, max_ub, heavy, h->num_sms));
+    void* scratch = scratch_bytes ? ar.alloc<unsigned char>(scratch_bytes, "heavy scratch") : nullptr;
+
+    for (int b = 1; b < kNumBins; ++b) launches += bin_count[b] > 0 ? 2 : 0;  // symbolic + numeric
+    launches += 3;                                                             // scan
+    for (int b = 1; b < kNumBins; ++b)
+        launch_symbolic(b, d_jobs, items + bin_off[b], bin_count[b], max_ub, scratch, scratch_bytes, &d_ctrl->stats,
+                        &d_ctrl->err, st, h->num_sms);
+    check_cuda(cudaGetLastError(), "K2 launch");
+    cudaEventRecord(h->ev[2], st);
+    int64_t* partials = ar.alloc<int64_t>(scan_partials_count(static_cast<int64_t>(slots)), "scan partials");
+    launch_scan(cnt, static_cast<int64_t>(slots) - 1, partials, st);
+    check_cuda(cudaGetLastError(), "K3 launch");
+    cudaEventRecord(h->ev[3], st);
+    check_cuda(cudaMemcpyAsync(&hc->totals[0], cnt + slots - 1, sizeof(int64_t), cudaMemcpyDeviceToHost, st),
+               "D2H total");
+    check_cuda(cudaMemcpyAsync(&hc->err, &d_ctrl->err, sizeof(ErrWord), cudaMemcpyDeviceToHost, st), "D2H err");
+    sync(h);  // sync 2: size of C
+    if (hc->err.code) {
+        std::string msg;
+        const spg_status s = map_err(hc->err, msg);
+        throw Failure{s, msg};
+    }
+    const int64_t sym_total = hc->totals[0];
+    if (h->cfg.hbm_budget_bytes &&
+        ar.bytes() + static_cast<size_t>(sym_total) * 12 > h->cfg.hbm_budget_bytes)
+        throw Failure{SPG_BUDGET_EXCEEDED, "product footprint exceeds the handle's HBM budget"};
+    int32_t* c_col = ar.alloc<int32_t>(static_cast<size_t>(sym_total), "C col");
+    double* c_val = ar.alloc<double>(static_cast<size_t>(sym_total), "C val");
+    for (int j = 0; j < njobs; ++j) {
+        jobs[j].c_col = c_col;
+        jobs[j].c_val = c_val;
+    }
+    check_cuda(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(Job) * njobs, cudaMemcpyHostToDevice, st), "H2D jobs");
+    for (int b = 1; b < kNumBins; ++b)
+        launch_numeric(b, d_jobs, items + bin_off[b], bin_count[b], max_ub, scratch, scratch_bytes, &d_ctrl->stats,
+                       &d_ctrl->err, st, h->num_sms);
+    check_cuda(cudaGetLastError(), "K4 launch");
+    cudaEventRecord(h->ev[4], st);
+    check_cuda(cudaMemcpyAsync(hc, d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, st), "D2H ctrl");
+    sync(h);  // sync 3: stored count
+    if (hc->err.code) {
+        std::string msg;
+        const spg_status s = map_err(hc->err, msg);
+        throw Failure{s, msg};
+    }
+    const int64_t nz_total = static_cast<int64_t>(hc->stats.nz_total);
+    int64_t* final_rp = cnt;
+    int32_t* final_col = c_col;
+    double* final_val = c_val;
+    if (nz_total != sym_total) {  // some sums were exact zeros: compact
+        launch_scan(nz, static_cast<int64_t>(slots) - 1, partials, st);
+        launches += 3 + njobs;
+        final_col = ar.alloc<int32_t>(static_cast<size_t>(nz_total), "C col (compact)");
+        final_val = ar.alloc<double>(static_cast<size_t>(nz_total), "C val (compact)");
+        for (int j = 0; j < njobs; ++j)
+            launch_compact(d_jobs + j, in[j].A->rows, final_col, final_val, st);
+        check_cuda(cudaGetLastError(), "K5 launch");
+        final_rp = nz;
+        ar.free_now(c_col);
+        ar.free_now(c_val);
+    }
+    cudaEventRecord(h->ev[5], st);
+
+    // results: offsets of job j start at final_rp[row_base_j + j]
+    std::vector<int64_t> starts(njobs + 1, 0);
+    starts[njobs] = nz_total;
+    if (njobs > 1) {
+        std::vector<int64_t> idx(njobs);
+        for (int j = 0; j < njobs; ++j) idx[j] = row_base[j] + j;
+        int64_t* d_idx = ar.alloc<int64_t>(static_cast<size_t>(njobs), "start index");
+        int64_t* d_starts = ar.alloc<int64_t>(static_cast<size_t>(njobs), "starts");
+        check_cuda(cudaMemcpyAsync(d_idx, idx.data(), sizeof(int64_t) * njobs, cudaMemcpyHostToDevice, st),
+                   "H2D start index");
+        launch_gather(final_rp, d_idx, d_starts, njobs, st);
+        launches += 2;  // gather + rebase
+        check_cuda(cudaMemcpyAsync(starts.data(), d_starts, sizeof(int64_t) * njobs, cudaMemcpyDeviceToHost, st),
+                   "D2H starts");
+        sync(h);
+    }
+    out.resize(njobs);
+    for (int j = 0; j < njobs; ++j) {
+        DevResult& r = out[j];
+        r.rows = in[j].A->rows;
+        r.cols = in[j].B->cols;
+        r.nnz = starts[j + 1] - starts[j];
+        if (njobs == 1) {
+            r.rp = final_rp;
+            r.ci = final_col;
+            r.v = final_val;
+            ar.release(final_rp);
+            ar.release(final_col);
+            ar.release(final_val);
+        } else {
+            r.rp = ar.alloc<int64_t>(static_cast<size_t>(r.rows) + 1, "result row_ptr");
+            r.ci = ar.alloc<int32_t>(static_cast<size_t>(r.nnz), "result col");
+            r.v = ar.alloc<double>(static_cast<size_t>(r.nnz), "result val");
+            check_cuda(cudaMemcpyAsync(r.ci, final_col + starts[j], sizeof(int32_t) * r.nnz, cudaMemcpyDeviceToDevice, st),
+                       "D2D col");
+            check_cuda(cudaMemcpyAsync(r.v, final_val + starts[j], sizeof(double) * r.nnz, cudaMemcpyDeviceToDevice, st),
+                       "D2D val");
+            check_cuda(cudaMemcpyAsync(r.rp, final_rp + row_base[j] + j, sizeof(int64_t) * (r.rows + 1),
+                                       cudaMemcpyDeviceToDevice, st), "D2D row_ptr");
+            ar.release(r.rp);
+            ar.release(r.ci);
+            ar.release(r.v);
+        }
+    }
+    if (njobs > 1) {  // every product's offsets start at zero
+        std::vector<RebaseItem> rb(njobs);
+        int64_t max_rows = 0;
+        for (int j = 0; j < njobs; ++j) {
+            rb[j] = RebaseItem{out[j].rp, starts[j], out[j].rows};
+            max_rows = std::max<int64_t>(max_rows, out[j].rows);
+        }
+        RebaseItem* d_rb = ar.alloc<RebaseItem>(static_cast<size_t>(njobs), "rebase items");
+        check_cuda(cudaMemcpyAsync(d_rb, rb.data(), sizeof(RebaseItem) * njobs, cudaMemcpyHostToDevice, st),
+                   "H2D rebase");
+        launch_rebase(d_rb, njobs, max_rows, st);
+        check_cuda(cudaGetLastError(), "rebase launch");
+        sync(h);  // rb / idx host vectors must outlive the copies
+    }
+    for (int j = 0; j < njobs; ++j) {
+        // per-product scalar products (for the FLOP count) are not split per job; report the batch total
+        out[j].products = njobs == 1 ? products : -1;
+    }
+    sync(h);
+    h->last.ms_rowwork = elapsed(h->ev[0], h->ev[1]);
+    h->last.ms_symbolic = elapsed(h->ev[1], h->ev[2]);
+    h->last.ms_scan = elapsed(h->ev[2], h->ev[3]);
+    h->last.ms_numeric = elapsed(h->ev[3], h->ev[4]);
+    h->last.ms_compact = elapsed(h->ev[4], h->ev[5]);
+    h->last.ms_total = elapsed(h->ev[0], h->ev[5]);
+    h->last.products = products;
+    h->last.nnz = nz_total;
+    h->last.rows = total_rows;
+    h->last.launches = launches;
+    for (int b = 0; b < kNumBins; ++b) h->last.bin_rows[b] = bin_count[b];
+}
+
+void free_result_arrays(spg_handle* h, spg_csr_result* c) {
+    if (!c) return;
+    if (c->location == SPG_DEVICE) {
+        if (c->row_ptr) cudaFreeAsync(c->row_ptr, h->stream);
+        if (c->col) cudaFreeAsync(c->col, h->stream);
+        if (c->val) cudaFreeAsync(c->val, h->stream);
+    } else {
+        std::free(c->row_ptr);
+        std::free(c->col);
+        std::free(c->val);
+    }
+    c->row_ptr = nullptr;
+    c->col = nullptr;
+    c->val = nullptr;
+    c->nnz = 0;
+}
+
+// Converts a device result into the caller's requested location.
+void deliver(spg_handle* h, DevResult& r, int32_t loc, spg_csr_result* C) {
+    std::memset(C, 0, sizeof(*C));
+    C->rows = r.rows;
+    C->cols = r.cols;
+    C->nnz = r.nnz;
+    C->products = r.products;
+    if (loc == SPG_DEVICE) {
+        C->location = SPG_DEVICE;
+        C->row_ptr = r.rp;
+        C->col = r.ci;
+        C->val = r.v;
+        return;
+    }
+    C->location = SPG_HOST;
+    C->row_ptr = static_cast<int64_t*>(std::malloc(sizeof(int64_t) * (static_cast<size_t>(r.rows) + 1)));
+    C->col = static_cast<int32_t*>(std::malloc(sizeof(int32_t) * std::max<int64_t>(r.nnz, 1)));
+    C->val = static_cast<double*>(std::malloc(sizeof(double) * std::max<int64_t>(r.nnz, 1)));
+    cudaError_t e = cudaSuccess;
+    if (!C->row_ptr || !C->col || !C->val) e = cudaErrorMemoryAllocation;
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(C->row_ptr, r.rp, sizeof(int64_t) * (static_cast<size_t>(r.rows) + 1),
+                            cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess && r.nnz)
+        e = cudaMemcpyAsync(C->col, r.ci, sizeof(int32_t) * r.nnz, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess && r.nnz)
+        e = cudaMemcpyAsync(C->val, r.v, sizeof(double) * r.nnz, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFreeAsync(r.rp, h->stream);
+    cudaFreeAsync(r.ci, h->stream);
+    cudaFreeAsync(r.v, h->stream);
+    if (e != cudaSuccess) {
+        free_result_arrays(h, C);
+        check_cuda(e, "D2H result");
+    }
+}
+
+template <typename F>
+spg_status guarded(spg_handle* h, F&& body) {
+    if (!h) return SPG_INVALID_ARGUMENT;
+    cudaSetDevice(h->device);
+    try {
+        body();
+        h->err.clear();
+        return SPG_OK;
+    } catch (const Failure& f) {
+        return fail(h, f.status, f.message);
+    } catch (const std::bad_alloc&) {
+        return fail(h, SPG_OUT_OF_MEMORY, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail(h, SPG_CUDA_ERROR, e.what());
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+extern "C" {
+
+spg_status spg_config_default(spg_config* c) {
+    if (!c) return SPG_INVALID_ARGUMENT;
+    std::memset(c, 0, sizeof(*c));
+    return SPG_OK;
+}
+
+spg_status spg_create(const spg_config* config, spg_handle** out) {
+    if (!out) return SPG_INVALID_ARGUMENT;
+    *out = nullptr;
+    spg_config cfg;
+    spg_config_default(&cfg);
+    if (config) cfg = *config;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return SPG_CUDA_ERROR;
+    }
+    if (cfg.device < 0 || cfg.device >= ndev) return SPG_INVALID_ARGUMENT;
+    auto* h = new spg_handle;
+    h->cfg = cfg;
+    h->device = cfg.device;
+    if (cudaSetDevice(h->device) != cudaSuccess || cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMallocHost(&h->ctrl, kCtrlBytes) != cudaSuccess) {
+        cudaGetLastError();
+        delete h;
+        return SPG_CUDA_ERROR;
+    }
+    cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
+    for (auto& e : h->ev) cudaEventCreate(&e);
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, h->device) == cudaSuccess) {
+        uint64_t threshold = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+    }
+    *out = h;
+    return SPG_OK;
+}
+
+void spg_destroy(spg_handle* h) {
+    if (!h) return;
+    cudaSetDevice(h->device);
+    if (h->acc_has) free_result_arrays(h, &h->acc);
+    cudaStreamSynchronize(h->stream);
+    for (auto& e : h->ev) cudaEventDestroy(e);
+    cudaStreamDestroy(h->stream);
+    cudaFreeHost(h->ctrl);
+    delete h;
+}
+
+const char* spg_last_error(const spg_handle* h) { return h ? h->err.c_str() : "NULL handle"; }
+
+const char* spg_status_string(spg_status s) {
+    switch (s) {
+        case SPG_OK: return "SPG_OK";
+        case SPG_INVALID_ARGUMENT: return "SPG_INVALID_ARGUMENT";
+        case SPG_OVERFLOW: return "SPG_OVERFLOW";
+        case SPG_OUT_OF_RANGE_COLUMN: return "SPG_OUT_OF_RANGE_COLUMN";
+        case SPG_OUT_OF_MEMORY: return "SPG_OUT_OF_MEMORY";
+        case SPG_BUDGET_EXCEEDED: return "SPG_BUDGET_EXCEEDED";
+        case SPG_DEVICE_TIMEOUT: return "SPG_DEVICE_TIMEOUT";
+        case SPG_CUDA_ERROR: return "SPG_CUDA_ERROR";
+        case SPG_NOT_READY: return "SPG_NOT_READY";
+        case SPG_CANCELLED: return "SPG_CANCELLED";
+    }
+    return "unknown spg_status";
+}
+
+void* spg_stream(spg_handle* h) { return h ? static_cast<void*>(h->stream) : nullptr; }
+
+spg_status spg_multiply(spg_handle* h, const spg_csr_view* A, const spg_csr_view* B, int32_t out_location,
+                        spg_csr_result* C) {
+    return guarded(h, [&] {
+        require(C != nullptr, SPG_INVALID_ARGUMENT, "C is NULL");
+        require(out_location == SPG_HOST || out_location == SPG_DEVICE, SPG_INVALID_ARGUMENT, "bad out_location");
+        std::vector<JobIn> in{{A, B, CsrView{}}};
+        std::vector<DevResult> out;
+        run_products(h, in, out, false, nullptr);
+        deliver(h, out[0], out_location, C);
+    });
+}
+
+spg_status spg_result_download(spg_handle* h, const spg_csr_result* C, int64_t* row_ptr, int32_t* col, double* val) {
+    return guarded(h, [&] {
+        require(C != nullptr && C->location == SPG_DEVICE, SPG_INVALID_ARGUMENT, "not a device result");
+        if (row_ptr)
+            check_cuda(cudaMemcpyAsync(row_ptr, C->row_ptr, sizeof(int64_t) * (static_cast<size_t>(C->rows) + 1),
+                                       cudaMemcpyDeviceToHost, h->stream), "D2H row_ptr");
+        if (col && C->nnz)
+            check_cuda(cudaMemcpyAsync(col, C->col, sizeof(int32_t) * C->nnz, cudaMemcpyDeviceToHost, h->stream),
+                       "D2H col");
+        if (val && C->nnz)
+            check_cuda(cudaMemcpyAsync(val, C->val, sizeof(double) * C->nnz, cudaMemcpyDeviceToHost, h->stream),
+                       "D2H val");
+        sync(h);
+    });
+}
+
+spg_status spg_result_free(spg_handle* h, spg_csr_result* C) {
+    return guarded(h, [&] { free_result_arrays(h, C); });
+}
+
+spg_status spg_scalar_multiplication_count(spg_handle* h, const spg_csr_view* A, const spg_csr_view* B,
+                                           int64_t* products) {
+    return guarded(h, [&] {
+        require(products != nullptr, SPG_INVALID_ARGUMENT, "products is NULL");
+        std::vector<JobIn> in{{A, B, CsrView{}}};
+        std::vector<DevResult> out;
+        run_products(h, in, out, true, products);
+    });
+}
+
+spg_status spg_last_timings(const spg_handle* h, spg_timings* t) {
+    if (!h || !t) return SPG_INVALID_ARGUMENT;
+    *t = h->last;
+    return SPG_OK;
+}
+
+spg_status spg_accum_begin(spg_handle* h, int32_t rows, int32_t cols) {
+    return guarded(h, [&] {
+        require(rows >= 0 && cols >= 0, SPG_INVALID_ARGUMENT, "negative accumulator shape");
+        if (h->acc_has) free_result_arrays(h, &h->acc);
+        h->acc_has = false;
+        h->acc_active = true;
+        h->acc_rows = rows;
+        h->acc_cols = cols;
+    });
+}
+
+spg_status spg_accum_add(spg_handle* h, const spg_csr_view* A, const spg_csr_view* B) {
+    return guarded(h, [&] {
+        require(h->acc_active, SPG_INVALID_ARGUMENT, "no accumulation in progress");
+        require(A && B, SPG_INVALID_ARGUMENT, "A or B is NULL");
+        require(A->cols == B->rows && A->rows == h->acc_rows && B->cols == h->acc_cols, SPG_INVALID_ARGUMENT,
+                "incompatible Trident partial product shapes");
+        CsrView S;
+        if (h->acc_has) {
+            S.rows = h->acc.rows;
+            S.cols = h->acc.cols;
+            S.nnz = h->acc.nnz;
+            S.rp = h->acc.row_ptr;
+            S.ci = h->acc.col;
+            S.v = h->acc.val;
+        }
+        std::vector<JobIn> in{{A, B, S}};
+        std::vector<DevResult> out;
+        run_products(h, in, out, false, nullptr);
+        if (h->acc_has) free_result_arrays(h, &h->acc);
+        deliver(h, out[0], SPG_DEVICE, &h->acc);
+        h->acc_has = true;
+    });
+}
+
+spg_status spg_accum_finish(spg_handle* h, int32_t out_location, spg_csr_result* C) {
+    return guarded(h, [&] {
+        require(h->acc_active, SPG_INVALID_ARGUMENT, "no accumulation in progress");
+        require(C != nullptr, SPG_INVALID_ARGUMENT, "C is NULL");
+        if (!h->acc_has) {  // no stage added: an all-empty result
+            DevResult r;
+            r.rows = h->acc_rows;
+            r.cols = h->acc_cols;
+            check_cuda(cudaMallocAsync(reinterpret_cast<void**>(&r.rp), sizeof(int64_t) * (r.rows + 1), h->stream),
+                       "alloc");
+            check_cuda(cudaMallocAsync(reinterpret_cast<void**>(&r.ci), 16, h->stream), "alloc");
+            check_cuda(cudaMallocAsync(reinterpret_cast<void**>(&r.v), 16, h->stream), "alloc");
+            check_cuda(cudaMemsetAsync(r.rp, 0, sizeof(int64_t) * (r.rows + 1), h->stream), "memset");
+            deliver(h, r, out_location, C);
+        } else {
+            DevResult r;
+            r.rows = h->acc.rows;
+            r.cols = h->acc.cols;
+            r.nnz = h->acc.nnz;
+            r.products = h->acc.products;
+            r.rp = h->acc.row_ptr;
+            r.ci = h->acc.col;
+            r.v = h->acc.val;
+            h->acc_has = false;
+            std::memset(&h->acc, 0, sizeof(h->acc));
+            deliver(h, r, out_location, C);
+        }
+        h->acc_active = false;
+    });
+}
+
+spg_status spg_multiply_batch(spg_handle* h, int32_t n, const spg_csr_view* A, const spg_csr_view* B,
+                              int32_t out_location, spg_csr_result* C) {
+    return guarded(h, [&] {
+        require(n >= 0 && (n == 0 || (A && B && C)), SPG_INVALID_ARGUMENT, "bad batch arguments");
+        require(out_location == SPG_HOST || out_location == SPG_DEVICE, SPG_INVALID_ARGUMENT, "bad out_location");
+        if (n == 0) return;
+        std::vector<JobIn> in(n);
+        for (int i = 0; i < n; ++i) in[i] = {&A[i], &B[i], CsrView{}};
+        std::vector<DevResult> out;
+        run_products(h, in, out, false, nullptr);
+        for (int i = 0; i < n; ++i) deliver(h, out[i], out_location, &C[i]);
+    });
+}
+
+void* spg_host_alloc(size_t bytes) {
+    void* p = nullptr;
+    if (cudaMallocHost(&p, bytes ? bytes : 16) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+
+void spg_host_free(void* p) {
+    if (p) cudaFreeHost(p);
+}
+
+}  // extern "C"

@@ -1,0 +1,539 @@
+// K4 numeric phase: every output row sorted, summed and written without zeros.
+//
+// For a row with P products the kernel
+//   1. enumerates the products in reference order (spg_enum.cuh): product t gets
+//      key = its column, seq = t, value = __dmul_rn(a, b) (one rounding, as
+//      `const double product = aValue * b` in spgemm_exchange.cpp:287);
+//   2. sorts (key, seq) pairs by key with a stable LSD radix sort (8-bit digits,
+//      ranks from __match_any_sync and per-warp digit counters; only the bits of
+//      max(col) - min(col) are sorted), so equal columns stay in product order;
+//   3. sums each run of equal columns sequentially in product order with
+//      __dadd_rn, starting from its first product (the `emplace` then `+=` of
+//      spgemm_exchange.cpp:288-293), and keeps the sums that are != 0.0
+//      (spgemm_exchange.cpp:304; NaN and infinities are kept);
+//   4. writes the kept (column, sum) pairs, already in column order, at the row's
+//      offset in C_tmp and the kept count into job.nz[row].
+// The result of every coordinate is therefore bit-identical to the serial
+// reference.  Rows of <= 512 products run one per warp, rows of <= 8192 one per
+// CTA with everything in shared memory, heavier rows one per CTA with the sort
+// in a global-memory slab.
+#include "spg_enum.cuh"
+
+namespace spg {
+namespace {
+
+template <int W>
+__device__ inline void row_sync() {
+    if (W == 1) __syncwarp();
+    else __syncthreads();
+}
+
+template <int W, int ITEMS>
+struct RowSmem {
+    static constexpr int kCap = W * 32 * ITEMS;
+    static constexpr int kSegN = W * 32;
+    double vals[kCap];          // product values by sequence number
+    SegTab<kSegN> seg;          // enumeration batch
+    int64_t warp_tmp[W + 1];    // block scans
+    uint32_t keys[kCap];        // columns, sorted in place
+    uint32_t hist[256 * W];     // digit counters, digit-major
+    uint32_t cnt[W * ITEMS];    // kept entries per (warp, item)
+    uint16_t seqs[kCap];        // sequence numbers, permuted with keys
+    int32_t red[2 * W];         // min / max column reduction
+};
+
+// Exclusive scan of n uint32 counters, each of the W*32 threads owning n/(W*32)
+// consecutive counters (n = 256*W: 8 each).
+template <int W>
+__device__ inline void scan_counters(uint32_t* c, int64_t* tmp) {
+    constexpr int kPer = 8;
+    const int lane = threadIdx.x & 31;
+    const int warp = W == 1 ? 0 : (threadIdx.x >> 5);
+    const int tid = W == 1 ? lane : threadIdx.x;
+    uint32_t v[kPer];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+        v[j] = c[tid * kPer + j];
+        sum += v[j];
+    }
+    uint32_t incl = warp_incl_scan(sum, lane);
+    uint32_t base = incl - sum;
+    if (W > 1) {
+        if (lane == 31) tmp[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            const uint32_t w = lane < W ? static_cast<uint32_t>(tmp[lane]) : 0u;
+            const uint32_t wi = warp_incl_scan(w, lane);
+            if (lane < W) tmp[lane] = wi - w;
+        }
+        __syncthreads();
+        base += static_cast<uint32_t>(tmp[warp]);
+    }
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+        c[tid * kPer + j] = base;
+        base += v[j];
+    }
+}
+
+// Stable rank of ITEMS striped items per lane against the per-warp digit
+// counters hist[d * W + warp] (which must start at zero).  rk[i] receives the
+// number of earlier items of this warp with the same digit.
+template <int W, int ITEMS>
+__device__ inline void rank_digits(const uint32_t (&dg)[ITEMS], uint32_t (&rk)[ITEMS], uint32_t* hist, int warp) {
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+        const unsigned peers = __match_any_sync(0xffffffffu, dg[i]);
+        const unsigned lt = peers & lanemask_lt();
+        const uint32_t base = hist[dg[i] * W + warp];
+        rk[i] = base + __popc(lt);
+        __syncwarp();
+        if (lt == 0) hist[dg[i] * W + warp] = base + __popc(peers);
+        __syncwarp();
+    }
+}
+
+template <int W, int ITEMS>
+__device__ void numeric_row(const Job& J, int row, RowSmem<W, ITEMS>& sm) {
+    constexpr int kCap = RowSmem<W, ITEMS>::kCap;
+    const int lane = threadIdx.x & 31;
+    const int warp = W == 1 ? 0 : (threadIdx.x >> 5);
+    const int tid = W == 1 ? lane : threadIdx.x;
+    const int P = static_cast<int>(J.ub[row]);
+
+    // 1. products into shared memory
+    int32_t lo = INT32_MAX, hi = INT32_MIN;
+    auto put = [&](int64_t seq, const int32_t* cp, const double* vp, double sc) {
+        const int32_t c = *cp;
+        sm.keys[seq] = static_cast<uint32_t>(c);
+        sm.seqs[seq] = static_cast<uint16_t>(seq);
+        sm.vals[seq] = __dmul_rn(sc, *vp);
+        lo = min(lo, c);
+        hi = max(hi, c);
+    };
+    if (W == 1) warp_products(J, row, *reinterpret_cast<SegTab<32>*>(&sm.seg), lane, put);
+    else block_products<W * 32>(J, row, sm.seg, sm.warp_tmp, put);
+    lo = warp_min(lo);
+    hi = warp_max(hi);
+    if (W > 1) {
+        if (lane == 0) {
+            sm.red[warp] = lo;
+            sm.red[W + warp] = hi;
+        }
+        __syncthreads();
+        lo = sm.red[0];
+        hi = sm.red[W];
+#pragma unroll
+        for (int w = 1; w < W; ++w) {
+            lo = min(lo, sm.red[w]);
+            hi = max(hi, sm.red[W + w]);
+        }
+    }
+    row_sync<W>();
+    const uint32_t cmin = static_cast<uint32_t>(lo);
+    const uint32_t range = static_cast<uint32_t>(hi - lo);
+    const int nbits = range ? 32 - __clz(range) : 0;
+
+    // 2. stable LSD radix sort of (key, seq) by key - cmin
+    for (int shift = 0; shift < nbits; shift += 8) {
+        uint32_t k[ITEMS], dg[ITEMS], rk[ITEMS];
+        uint16_t s[ITEMS];
+        for (int d = tid; d < 256 * W; d += W * 32) sm.hist[d] = 0;
+        row_sync<W>();
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i) {
+            const int pos = (warp * ITEMS + i) * 32 + lane;
+            const bool valid = pos < P;
+            k[i] = valid ? sm.keys[pos] : 0u;
+            s[i] = valid ? sm.seqs[pos] : uint16_t{0};
+            dg[i] = valid ? (((k[i] - cmin) >> shift) & 255u) : 255u;
+        }
+        rank_digits<W, ITEMS>(dg, rk, sm.hist, warp);
+        row_sync<W>();
+        scan_counters<W>(sm.hist, sm.warp_tmp);
+        row_sync<W>();
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i) {
+            const uint32_t dst = sm.hist[dg[i] * W + warp] + rk[i];
+            if (dst < static_cast<uint32_t>(P)) {
+                sm.keys[dst] = k[i];
+                sm.seqs[dst] = s[i];
+            }
+        }
+        row_sync<W>();
+    }
+
+    // 3. runs of equal columns, summed in product order
+    double sum[ITEMS];
+    uint32_t col[ITEMS];
+    unsigned keepmask[ITEMS];
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+        const int pos = (warp * ITEMS + i) * 32 + lane;
+        bool keep = false;
+        sum[i] = 0.0;
+        col[i] = 0;
+        if (pos < P) {
+            const uint32_t key = sm.keys[pos];
+            if (pos == 0 || sm.keys[pos - 1] != key) {
+                double acc = sm.vals[sm.seqs[pos]];
+                for (int q = pos + 1; q < P && sm.keys[q] == key; ++q) acc = __dadd_rn(acc, sm.vals[sm.seqs[q]]);
+                sum[i] = acc;
+                col[i] = key;
+                keep = acc != 0.0;
+            }
+        }
+        keepmask[i] = __ballot_sync(0xffffffffu, keep);
+        if (lane == 0) sm.cnt[warp * ITEMS + i] = __popc(keepmask[i]);
+    }
+    row_sync<W>();
+    // exclusive scan of the W*ITEMS kept counts by warp 0
+    constexpr int kN = W * ITEMS;
+    constexpr int kPer = (kN + 31) / 32;
+    if (warp == 0) {
+        uint32_t v[kPer];
+        uint32_t tot = 0;
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            const int idx = lane * kPer + j;
+            v[j] = idx < kN ? sm.cnt[idx] : 0u;
+            tot += v[j];
+        }
+        const uint32_t incl = warp_incl_scan(tot, lane);
+        uint32_t base = incl - tot;
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            const int idx = lane * kPer + j;
+            if (idx < kN) sm.cnt[idx] = base;
+            base += v[j];
+        }
+        if (lane == 31) sm.red[0] = static_cast<int32_t>(incl);
+    }
+    row_sync<W>();
+    const int64_t out0 = J.cnt[row];
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+        if (keepmask[i] & (1u << lane)) {
+            const int64_t idx = out0 + sm.cnt[warp * ITEMS + i] + __popc(keepmask[i] & lanemask_lt());
+            J.c_col[idx] = static_cast<int32_t>(col[i]);
+            J.c_val[idx] = sum[i];
+        }
+    }
+    if (tid == 0) J.nz[row] = sm.red[0];
+    row_sync<W>();
+}
+
+constexpr int kWarpKernelThreads = 256;
+
+template <int ITEMS>
+__global__ void __launch_bounds__(kWarpKernelThreads)
+num_warp_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items, int64_t count,
+                Stats* __restrict__ stats) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    using Sm = RowSmem<1, ITEMS>;
+    Sm& sm = reinterpret_cast<Sm*>(smem_raw)[threadIdx.x >> 5];
+    __shared__ unsigned long long s_nz;
+    if (threadIdx.x == 0) s_nz = 0;
+    __syncthreads();
+    const int64_t warps = static_cast<int64_t>(gridDim.x) * (kWarpKernelThreads / 32);
+    unsigned long long mine = 0;
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * (kWarpKernelThreads / 32) + (threadIdx.x >> 5); i < count;
+         i += warps) {
+        const int64_t it = items[i];
+        const Job& J = jobs[item_job(it)];
+        const int row = item_row(it);
+        numeric_row<1, ITEMS>(J, row, sm);
+        if ((threadIdx.x & 31) == 0) mine += static_cast<unsigned long long>(J.nz[row]);
+    }
+    if ((threadIdx.x & 31) == 0 && mine) atomicAdd(&s_nz, mine);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_nz) atomicAdd(&stats->nz_total, s_nz);
+}
+
+template <int W, int ITEMS>
+__global__ void __launch_bounds__(W * 32)
+num_block_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items, int64_t count,
+                 Stats* __restrict__ stats) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    using Sm = RowSmem<W, ITEMS>;
+    Sm& sm = *reinterpret_cast<Sm*>(smem_raw);
+    unsigned long long mine = 0;
+    for (int64_t i = blockIdx.x; i < count; i += gridDim.x) {
+        const int64_t it = items[i];
+        const Job& J = jobs[item_job(it)];
+        const int row = item_row(it);
+        numeric_row<W, ITEMS>(J, row, sm);
+        if (threadIdx.x == 0) mine += static_cast<unsigned long long>(J.nz[row]);
+    }
+    if (threadIdx.x == 0 && mine) atomicAdd(&stats->nz_total, mine);
+}
+
+// ---------------------------------------------------------------------------
+// Heavy rows: one CTA per row, the sort in a global-memory slab of this CTA.
+constexpr int kHeavyW = 16;
+constexpr int kHeavyItems = 16;
+constexpr int kHeavyThreads = kHeavyW * 32;
+constexpr int kHeavyTile = kHeavyThreads * kHeavyItems;
+
+struct HeavySmem {
+    SegTab<kHeavyThreads> seg;
+    int64_t warp_tmp[kHeavyW + 1];
+    uint32_t hist[256 * kHeavyW];
+    uint32_t digit_base[256];
+    uint32_t digit_tot[256];
+    uint32_t cnt[kHeavyW * kHeavyItems];
+    int32_t red[2 * kHeavyW];
+    uint32_t out_base;
+};
+
+struct HeavySlab {
+    uint32_t* keys[2];
+    uint32_t* seqs[2];
+    double* vals;
+};
+
+__device__ inline HeavySlab heavy_slab(void* base, int64_t cap, int cta) {
+    // per CTA: vals (8*cap) | keys0 | keys1 | seqs0 | seqs1 (4*cap each)
+    unsigned char* p = static_cast<unsigned char*>(base) + static_cast<size_t>(cta) * 24 * static_cast<size_t>(cap);
+    HeavySlab s;
+    s.vals = reinterpret_cast<double*>(p);
+    s.keys[0] = reinterpret_cast<uint32_t*>(p + 8 * cap);
+    s.keys[1] = s.keys[0] + cap;
+    s.seqs[0] = s.keys[1] + cap;
+    s.seqs[1] = s.seqs[0] + cap;
+    return s;
+}
+
+__global__ void __launch_bounds__(kHeavyThreads)
+num_heavy_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items, int64_t count, void* slabs,
+                 int64_t cap, Stats* __restrict__ stats) {
+    __shared__ HeavySmem sm;
+    const HeavySlab sl = heavy_slab(slabs, cap, blockIdx.x);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, tid = threadIdx.x;
+    unsigned long long kept_total = 0;
+    for (int64_t it_i = blockIdx.x; it_i < count; it_i += gridDim.x) {
+        const int64_t it = items[it_i];
+        const Job& J = jobs[item_job(it)];
+        const int row = item_row(it);
+        const int64_t P = J.ub[row];
+
+        int32_t lo = INT32_MAX, hi = INT32_MIN;
+        block_products<kHeavyThreads>(J, row, sm.seg, sm.warp_tmp,
+                                      [&](int64_t seq, const int32_t* cp, const double* vp, double sc) {
+            const int32_t c = *cp;
+            sl.keys[0][seq] = static_cast<uint32_t>(c);
+            sl.seqs[0][seq] = static_cast<uint32_t>(seq);
+            sl.vals[seq] = __dmul_rn(sc, *vp);
+            lo = min(lo, c);
+            hi = max(hi, c);
+        });
+        lo = warp_min(lo);
+        hi = warp_max(hi);
+        if (lane == 0) {
+            sm.red[warp] = lo;
+            sm.red[kHeavyW + warp] = hi;
+        }
+        __syncthreads();
+        lo = sm.red[0];
+        hi = sm.red[kHeavyW];
+        for (int w = 1; w < kHeavyW; ++w) {
+            lo = min(lo, sm.red[w]);
+            hi = max(hi, sm.red[kHeavyW + w]);
+        }
+        __syncthreads();
+        const uint32_t cmin = static_cast<uint32_t>(lo);
+        const uint32_t range = static_cast<uint32_t>(hi - lo);
+        const int nbits = range ? 32 - __clz(range) : 0;
+        int cur = 0;
+        const int64_t ntiles = (P + kHeavyTile - 1) / kHeavyTile;
+
+        for (int shift = 0; shift < nbits; shift += 8) {
+            const uint32_t* kin = sl.keys[cur];
+            const uint32_t* sin = sl.seqs[cur];
+            uint32_t* kout = sl.keys[cur ^ 1];
+            uint32_t* sout = sl.seqs[cur ^ 1];
+            // digit totals of the whole row
+            if (tid < 256) sm.digit_tot[tid] = 0;
+            __syncthreads();
+            for (int64_t p = tid; p < P; p += kHeavyThreads)
+                atomicAdd(&sm.digit_tot[((kin[p] - cmin) >> shift) & 255u], 1u);
+            __syncthreads();
+            if (warp == 0) {  // exclusive scan of 256 totals, 8 per lane
+                uint32_t v[8], tot = 0;
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    v[j] = sm.digit_tot[lane * 8 + j];
+                    tot += v[j];
+                }
+                uint32_t base = warp_incl_scan(tot, lane) - tot;
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    sm.digit_base[lane * 8 + j] = base;
+                    base += v[j];
+                }
+            }
+            __syncthreads();
+            for (int64_t t = 0; t < ntiles; ++t) {
+                const int64_t tile0 = t * kHeavyTile;
+                uint32_t k[kHeavyItems], s[kHeavyItems], dg[kHeavyItems], rk[kHeavyItems];
+                for (int d = tid; d < 256 * kHeavyW; d += kHeavyThreads) sm.hist[d] = 0;
+                __syncthreads();
+#pragma unroll
+                for (int i = 0; i < kHeavyItems; ++i) {
+                    const int64_t pos = tile0 + (warp * kHeavyItems + i) * 32 + lane;
+                    const bool valid = pos < P;
+                    k[i] = valid ? kin[pos] : 0u;
+                    s[i] = valid ? sin[pos] : 0u;
+                    dg[i] = valid ? (((k[i] - cmin) >> shift) & 255u) : 255u;
+                }
+                rank_digits<kHeavyW, kHeavyItems>(dg, rk, sm.hist, warp);
+                __syncthreads();
+                if (tid < 256) {  // this tile's count of digit tid (padding included)
+                    uint32_t c = 0;
+#pragma unroll
+                    for (int w = 0; w < kHeavyW; ++w) c += sm.hist[tid * kHeavyW + w];
+                    sm.digit_tot[tid] = c;
+                }
+                __syncthreads();
+                scan_counters<kHeavyW>(sm.hist, sm.warp_tmp);
+                __syncthreads();
+#pragma unroll
+                for (int i = 0; i < kHeavyItems; ++i) {
+                    const int64_t pos = tile0 + (warp * kHeavyItems + i) * 32 + lane;
+                    if (pos < P) {
+                        // within-tile position of this item among its digit, then the row-wide base
+                        const uint32_t within = sm.hist[dg[i] * kHeavyW + warp] + rk[i] - sm.hist[dg[i] * kHeavyW];
+                        const uint32_t dst = sm.digit_base[dg[i]] + within;
+                        kout[dst] = k[i];
+                        sout[dst] = s[i];
+                    }
+                }
+                __syncthreads();
+                if (tid < 256) sm.digit_base[tid] += sm.digit_tot[tid] - (tid == 255 ? static_cast<uint32_t>(
+                    (tile0 + kHeavyTile > P) ? (tile0 + kHeavyTile - P) : 0) : 0u);
+                __syncthreads();
+            }
+            cur ^= 1;
+        }
+
+        // runs and output, tile by tile
+        const uint32_t* keys = sl.keys[cur];
+        const uint32_t* seqs = sl.seqs[cur];
+        if (tid == 0) sm.out_base = 0;
+        __syncthreads();
+        const int64_t out0 = J.cnt[row];
+        for (int64_t t = 0; t < ntiles; ++t) {
+            const int64_t tile0 = t * kHeavyTile;
+            double sum[kHeavyItems];
+            uint32_t col[kHeavyItems];
+            unsigned keepmask[kHeavyItems];
+#pragma unroll
+            for (int i = 0; i < kHeavyItems; ++i) {
+                const int64_t pos = tile0 + (warp * kHeavyItems + i) * 32 + lane;
+                bool keep = false;
+                sum[i] = 0.0;
+                col[i] = 0;
+                if (pos < P) {
+                    const uint32_t key = keys[pos];
+                    if (pos == 0 || keys[pos - 1] != key) {
+                        double acc = sl.vals[seqs[pos]];
+                        for (int64_t q = pos + 1; q < P && keys[q] == key; ++q) acc = __dadd_rn(acc, sl.vals[seqs[q]]);
+                        sum[i] = acc;
+                        col[i] = key;
+                        keep = acc != 0.0;
+                    }
+                }
+                keepmask[i] = __ballot_sync(0xffffffffu, keep);
+                if (lane == 0) sm.cnt[warp * kHeavyItems + i] = __popc(keepmask[i]);
+            }
+            __syncthreads();
+            if (warp == 0) {  // 256 counts, 8 per lane
+                uint32_t v[8], tot = 0;
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    v[j] = sm.cnt[lane * 8 + j];
+                    tot += v[j];
+                }
+                const uint32_t incl = warp_incl_scan(tot, lane);
+                uint32_t base = incl - tot;
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    sm.cnt[lane * 8 + j] = base;
+                    base += v[j];
+                }
+                if (lane == 31) sm.red[0] = static_cast<int32_t>(incl);
+            }
+            __syncthreads();
+            const int64_t tile_out = out0 + sm.out_base;
+#pragma unroll
+            for (int i = 0; i < kHeavyItems; ++i) {
+                if (keepmask[i] & (1u << lane)) {
+                    const int64_t idx = tile_out + sm.cnt[warp * kHeavyItems + i] + __popc(keepmask[i] & lanemask_lt());
+                    J.c_col[idx] = static_cast<int32_t>(col[i]);
+                    J.c_val[idx] = sum[i];
+                }
+            }
+            __syncthreads();
+            if (tid == 0) sm.out_base += static_cast<uint32_t>(sm.red[0]);
+            __syncthreads();
+        }
+        if (tid == 0) {
+            J.nz[row] = sm.out_base;
+            kept_total += sm.out_base;
+        }
+        __syncthreads();
+    }
+    if (tid == 0 && kept_total) atomicAdd(&stats->nz_total, kept_total);
+}
+
+int capped(int64_t work, int per_block, int cap) {
+    const int64_t g = (work + per_block - 1) / per_block;
+    return static_cast<int>(g < 1 ? 1 : (g > cap ? cap : g));
+}
+
+int heavy_grid(int64_t count, int num_sms) { return static_cast<int>(count < num_sms ? count : num_sms); }
+
+template <int ITEMS>
+void run_warp(const Job* jobs, const int64_t* items, int64_t count, Stats* stats, cudaStream_t st, int num_sms) {
+    const int smem = 8 * static_cast<int>(sizeof(RowSmem<1, ITEMS>));
+    cudaFuncSetAttribute(num_warp_kernel<ITEMS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    num_warp_kernel<ITEMS><<<capped(count, 8, num_sms * 16), kWarpKernelThreads, smem, st>>>(jobs, items, count, stats);
+}
+
+template <int W, int ITEMS>
+void run_block(const Job* jobs, const int64_t* items, int64_t count, Stats* stats, cudaStream_t st, int num_sms) {
+    const int smem = static_cast<int>(sizeof(RowSmem<W, ITEMS>));
+    cudaFuncSetAttribute(num_block_kernel<W, ITEMS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    num_block_kernel<W, ITEMS><<<capped(count, 1, num_sms * 8), W * 32, smem, st>>>(jobs, items, count, stats);
+}
+
+}  // namespace
+
+size_t numeric_scratch_bytes(int bin, int64_t max_ub, int64_t count, int num_sms) {
+    if (bin != kBinHeavy || count == 0) return 0;
+    return static_cast<size_t>(heavy_grid(count, num_sms)) * 24 * static_cast<size_t>(max_ub);
+}
+
+void launch_numeric(int bin, const Job* d_jobs, const int64_t* d_items, int64_t count, int64_t max_ub,
+                    void* d_scratch, size_t, Stats* d_stats, ErrWord*, cudaStream_t st, int num_sms) {
+    if (count <= 0) return;
+    switch (bin) {
+        case kBinW1: run_warp<1>(d_jobs, d_items, count, d_stats, st, num_sms); break;
+        case kBinW2: run_warp<2>(d_jobs, d_items, count, d_stats, st, num_sms); break;
+        case kBinW4: run_warp<4>(d_jobs, d_items, count, d_stats, st, num_sms); break;
+        case kBinW8: run_warp<8>(d_jobs, d_items, count, d_stats, st, num_sms); break;
+        case kBinW16: run_warp<16>(d_jobs, d_items, count, d_stats, st, num_sms); break;
+        case kBinB1K: run_block<4, 8>(d_jobs, d_items, count, d_stats, st, num_sms); break;
+        case kBinB2K: run_block<8, 8>(d_jobs, d_items, count, d_stats, st, num_sms); break;
+        case kBinB4K: run_block<8, 16>(d_jobs, d_items, count, d_stats, st, num_sms); break;
+        case kBinB8K: run_block<16, 16>(d_jobs, d_items, count, d_stats, st, num_sms); break;
+        case kBinHeavy:
+            num_heavy_kernel<<<heavy_grid(count, num_sms), kHeavyThreads, 0, st>>>(d_jobs, d_items, count, d_scratch,
+                                                                                   max_ub, d_stats);
+            break;
+        default: break;
+    }
+}
+
+}  // namespace spg

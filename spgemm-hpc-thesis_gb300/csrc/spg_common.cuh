@@ -1,0 +1,199 @@
+// Shared definitions of the GB300 SpGEMM engine (device side and launchers).
+//
+// The engine computes C = S + A*B row by row (S is an optional addend used by
+// the accumulate mode; a plain product has no S).  Every output coordinate is
+// the sequential FP64 sum of its products in the reference's order: the S entry
+// first, then A entries in stored order, then B entries in stored order, each
+// product rounded once (__dmul_rn) and added with one rounding (__dadd_rn).
+// This is the traversal of serialSpgemm (spgemm_common.cpp:131-178) and of the
+// baseline spgemm() row loop (spgemm_exchange.cpp:279-309), so results are
+// bit-identical to the reference's serial product.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace spg {
+
+constexpr int kWarp = 32;
+
+// Read-only CSR view in device memory (int64 row offsets, int32 columns, FP64).
+struct CsrView {
+    int32_t rows = 0, cols = 0;
+    int64_t nnz = 0;
+    const int64_t* rp = nullptr;
+    const int32_t* ci = nullptr;
+    const double* v = nullptr;
+};
+
+// One product of a launch.  Batched launches carry many jobs; every work item
+// names a job and a row.
+struct Job {
+    CsrView A, B, S;          // S.rp == nullptr: no addend
+    int64_t* ub = nullptr;    // [A.rows]  products per row (upper bound of its nnz)
+    int64_t* cnt = nullptr;   // [A.rows+1] distinct columns per row, scanned in place into C_tmp offsets
+    int64_t* nz = nullptr;    // [A.rows+1] stored (nonzero) entries per row
+    int32_t* c_col = nullptr; // C_tmp columns (size = total of cnt)
+    double* c_val = nullptr;  // C_tmp values
+    int64_t row_base = 0;     // first flattened row of this job in a batch
+};
+
+// Row bins by product count (ub).  Bin b covers (kBinHi[b-1], kBinHi[b]].
+enum Bin : int {
+    kBinEmpty = 0,
+    kBinW1,    // <= 32       warp, 1 item per lane
+    kBinW2,    // <= 64       warp, 2 items
+    kBinW4,    // <= 128
+    kBinW8,    // <= 256
+    kBinW16,   // <= 512
+    kBinB1K,   // <= 1024     4 warps x 8 items
+    kBinB2K,   // <= 2048     8 warps x 8 items
+    kBinB4K,   // <= 4096     8 warps x 16 items
+    kBinB8K,   // <= 8192     16 warps x 16 items
+    kBinHeavy, // >  8192     one CTA per row, sort in global memory
+    kNumBins
+};
+constexpr int64_t kHeavyThreshold = 8192;
+
+__host__ __device__ inline int clz64(unsigned long long x) {
+#ifdef __CUDA_ARCH__
+    return __clzll(static_cast<long long>(x));
+#else
+    return x ? __builtin_clzll(x) : 64;
+#endif
+}
+
+// 0 for ub == 0, kBinHeavy above kHeavyThreshold, else max(1, ceil(log2 ub) - 4).
+__host__ __device__ inline int bin_of(int64_t ub) {
+    if (ub <= 0) return kBinEmpty;
+    if (ub > kHeavyThreshold) return kBinHeavy;
+    if (ub <= 32) return kBinW1;
+    return (64 - clz64(static_cast<unsigned long long>(ub - 1))) - 4;
+}
+
+// Largest product count of a bin (its capacity).
+__host__ __device__ inline int64_t bin_capacity(int b) {
+    return b == kBinEmpty ? 0 : (b == kBinHeavy ? INT64_MAX : (int64_t{16} << b));
+}
+
+// Error word written by kernels (first error wins) and read by the host at
+// each synchronisation point.
+struct ErrWord {
+    int32_t code;    // spg_status value, 0 = none
+    int32_t where;   // kernel tag
+    int64_t detail;  // offending row / entry / value
+};
+
+enum ErrCode : int32_t {
+    kErrNone = 0,
+    kErrInvalid = 1,        // malformed CSR or column outside the matrix
+    kErrOverflow = 2,       // a count that does not fit
+    kErrColumnRange = 3,    // A column outside B's rows
+};
+
+// Device-side counters collected per launch (reset by the host).
+struct Stats {
+    unsigned long long products;      // sum of ub over all rows (the FLOP count / 2)
+    unsigned long long max_ub;        // largest ub
+    unsigned long long bin_count[kNumBins];
+    unsigned long long sym_total;     // sum of cnt
+    unsigned long long nz_total;      // sum of nz
+};
+
+__device__ inline void raise_error(ErrWord* e, int32_t code, int32_t where, int64_t detail) {
+    if (atomicCAS(&e->code, 0, code) == 0) {
+        e->where = where;
+        e->detail = detail;
+    }
+}
+
+__device__ inline unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+template <typename T>
+__device__ inline T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <typename T>
+__device__ inline T warp_min(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        T w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w < v ? w : v;
+    }
+    return v;
+}
+
+template <typename T>
+__device__ inline T warp_max(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        T w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
+}
+
+// Inclusive warp scan.
+template <typename T>
+__device__ inline T warp_incl_scan(T v, int lane) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        T w = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += w;
+    }
+    return v;
+}
+
+// Work item: job index in the high 32 bits, row in the low 32 bits.
+__host__ __device__ inline int64_t make_item(int job, int row) {
+    return (static_cast<int64_t>(job) << 32) | static_cast<uint32_t>(row);
+}
+__host__ __device__ inline int item_job(int64_t it) { return static_cast<int>(it >> 32); }
+__host__ __device__ inline int item_row(int64_t it) { return static_cast<int>(it & 0xffffffff); }
+
+// --------------------------------------------------------------------------
+// Host-side launchers (one per phase).  All are asynchronous on `stream`.
+
+// K1: products per row (ub), bin histogram, product total and input checks.
+// Rows of all jobs are flattened: job j owns rows [row_base_j, row_base_j + A_j.rows).
+void launch_rowwork(const Job* d_jobs, int njobs, const int64_t* d_job_row_base, int64_t total_rows,
+                    Stats* d_stats, ErrWord* d_err, cudaStream_t stream);
+// K1b: scatter work items into per-bin lists (d_bin_off from the bin histogram).
+void launch_bin_scatter(const Job* d_jobs, int njobs, const int64_t* d_job_row_base, int64_t total_rows,
+                        const int64_t* d_bin_off, unsigned long long* d_bin_cursor, int64_t* d_items,
+                        cudaStream_t stream);
+// K2: distinct columns per row into job.cnt[row] for the items of one bin.
+void launch_symbolic(int bin, const Job* d_jobs, const int64_t* d_items, int64_t count, int64_t max_ub,
+                     void* d_scratch, size_t scratch_bytes, Stats* d_stats, ErrWord* d_err,
+                     cudaStream_t stream, int num_sms);
+size_t symbolic_scratch_bytes(int bin, int64_t max_ub, int64_t count, int num_sms);
+// K3: exclusive scan of n+1 int64 counts in place (last entry becomes the total).
+void launch_scan(int64_t* d_data, int64_t n, int64_t* d_partials, cudaStream_t stream);
+size_t scan_partials_count(int64_t n);
+// K4: sorted, summed, zero-free rows into job.c_col/c_val and job.nz[row].
+void launch_numeric(int bin, const Job* d_jobs, const int64_t* d_items, int64_t count, int64_t max_ub,
+                    void* d_scratch, size_t scratch_bytes, Stats* d_stats, ErrWord* d_err,
+                    cudaStream_t stream, int num_sms);
+size_t numeric_scratch_bytes(int bin, int64_t max_ub, int64_t count, int num_sms);
+// K5: move rows from C_tmp (offsets job.cnt) to C (offsets job.nz, scanned).
+void launch_compact(const Job* d_job, int rows, int32_t* out_col, double* out_val, cudaStream_t stream);
+// Bin list offsets from the bin histogram.
+void launch_bin_offsets(const Stats* d_stats, int64_t* d_bin_off, cudaStream_t stream);
+
+// Batched results: dst[i] = src[idx[i]] and per-product offset rebasing.
+struct RebaseItem {
+    int64_t* rp;     // rows + 1 offsets of one product
+    int64_t start;   // subtracted from every offset
+    int64_t rows;
+};
+void launch_gather(const int64_t* d_src, const int64_t* d_idx, int64_t* d_dst, int n, cudaStream_t stream);
+void launch_rebase(const RebaseItem* d_items, int n, int64_t max_rows, cudaStream_t stream);
+
+}  // namespace spg

@@ -1,0 +1,159 @@
+// Enumeration of the scalar products of one output row in the reference order.
+//
+// A row's products are the concatenation of "segments": the addend row S_i
+// (scale 1.0) when present, then, for every A entry (k, a) in stored order, the
+// B row k scaled by a.  Product number t of the row (its sequence number) is
+// the t-th element of that concatenation, which is the order in which
+// serialSpgemm (spgemm_common.cpp:139-152) and spgemm() (spgemm_exchange.cpp:
+// 279-294) visit them.
+//
+// Segments are processed in batches of one per thread: the batch's segment
+// lengths are scanned, their descriptors are staged in shared memory, and the
+// threads then stride over the batch's products, so that neighbouring threads
+// read neighbouring B entries (coalesced) whatever the segment lengths are.
+#pragma once
+
+#include "spg_common.cuh"
+
+namespace spg {
+
+template <int N>
+struct SegTab {
+    const int32_t* colp[N];
+    const double* valp[N];
+    double scale[N];
+    int64_t incl[N];  // inclusive prefix of segment lengths within the batch
+};
+
+// Segment e of a row (e counts the addend first when present).
+__device__ inline void row_segment(const Job& J, int row, int64_t a0, bool has_s, int64_t e,
+                                   const int32_t*& cp, const double*& vp, double& sc, int64_t& len) {
+    if (has_s && e == 0) {
+        const int64_t s0 = J.S.rp[row];
+        cp = J.S.ci + s0;
+        vp = J.S.v + s0;
+        sc = 1.0;
+        len = J.S.rp[row + 1] - s0;
+    } else {
+        const int64_t p = a0 + e - (has_s ? 1 : 0);
+        const int32_t k = J.A.ci[p];
+        const int64_t b0 = J.B.rp[k];
+        cp = J.B.ci + b0;
+        vp = J.B.v + b0;
+        sc = J.A.v[p];
+        len = J.B.rp[k + 1] - b0;
+    }
+}
+
+// Smallest j in [0, N) with incl[j] > t (the batch total exceeds t).
+template <int N>
+__device__ inline int seg_search(const int64_t* incl, int64_t t) {
+    int j = 0;
+#pragma unroll
+    for (int step = N / 2; step >= 1; step >>= 1)
+        if (incl[j + step - 1] <= t) j += step;
+    return j;
+}
+
+// Warp-cooperative enumeration.  f(seq, colp, valp, scale) is called once per
+// product by the lane that owns it; lanes own products t = lane, lane+32, ...
+// of each batch.  All 32 lanes must call this together.
+template <typename F>
+__device__ inline void warp_products(const Job& J, int row, SegTab<32>& tab, int lane, F&& f) {
+    const bool has_s = J.S.rp != nullptr;
+    const int64_t a0 = J.A.rp[row];
+    const int64_t nseg = (J.A.rp[row + 1] - a0) + (has_s ? 1 : 0);
+    int64_t seq_base = 0;
+    for (int64_t e0 = 0; e0 < nseg; e0 += 32) {
+        const int64_t e = e0 + lane;
+        const int32_t* cp = nullptr;
+        const double* vp = nullptr;
+        double sc = 1.0;
+        int64_t len = 0;
+        if (e < nseg) row_segment(J, row, a0, has_s, e, cp, vp, sc, len);
+        const int64_t incl = warp_incl_scan(len, lane);
+        tab.colp[lane] = cp;
+        tab.valp[lane] = vp;
+        tab.scale[lane] = sc;
+        tab.incl[lane] = incl;
+        __syncwarp();
+        const int64_t total = tab.incl[31];
+        if (lane < total) {
+            int j = seg_search<32>(tab.incl, lane);
+            for (int64_t t = lane; t < total; t += 32) {
+                while (tab.incl[j] <= t) ++j;
+                const int64_t q = t - (j ? tab.incl[j - 1] : 0);
+                f(seq_base + t, tab.colp[j] + q, tab.valp[j] + q, tab.scale[j]);
+            }
+        }
+        seq_base += total;
+        __syncwarp();
+    }
+}
+
+// Inclusive block scan of int64 (NT threads, NT/32 <= 32 warps).
+template <int NT>
+__device__ inline int64_t block_incl_scan(int64_t v, int64_t* s_warp /* NT/32 + 1 */) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int NW = NT / 32;
+    const int64_t incl = warp_incl_scan(v, lane);
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        const int64_t w = lane < NW ? s_warp[lane] : 0;
+        const int64_t wi = warp_incl_scan(w, lane);
+        if (lane < NW) s_warp[lane] = wi - w;
+    }
+    __syncthreads();
+    const int64_t out = incl + s_warp[warp];
+    __syncthreads();
+    return out;
+}
+
+// Block-cooperative enumeration (all NT threads call it together).  Threads
+// own products t = tid, tid+NT, ... of each batch of NT segments.
+template <int NT, typename F>
+__device__ inline void block_products(const Job& J, int row, SegTab<NT>& tab, int64_t* s_warp, F&& f) {
+    const int tid = threadIdx.x;
+    const bool has_s = J.S.rp != nullptr;
+    const int64_t a0 = J.A.rp[row];
+    const int64_t nseg = (J.A.rp[row + 1] - a0) + (has_s ? 1 : 0);
+    int64_t seq_base = 0;
+    for (int64_t e0 = 0; e0 < nseg; e0 += NT) {
+        const int64_t e = e0 + tid;
+        const int32_t* cp = nullptr;
+        const double* vp = nullptr;
+        double sc = 1.0;
+        int64_t len = 0;
+        if (e < nseg) row_segment(J, row, a0, has_s, e, cp, vp, sc, len);
+        const int64_t incl = block_incl_scan<NT>(len, s_warp);
+        tab.colp[tid] = cp;
+        tab.valp[tid] = vp;
+        tab.scale[tid] = sc;
+        tab.incl[tid] = incl;
+        __syncthreads();
+        const int64_t total = tab.incl[NT - 1];
+        if (tid < total) {
+            int j = seg_search<NT>(tab.incl, tid);
+            for (int64_t t = tid; t < total; t += NT) {
+                while (tab.incl[j] <= t) ++j;
+                const int64_t q = t - (j ? tab.incl[j - 1] : 0);
+                f(seq_base + t, tab.colp[j] + q, tab.valp[j] + q, tab.scale[j]);
+            }
+        }
+        seq_base += total;
+        __syncthreads();
+    }
+}
+
+__device__ inline uint32_t hash_slot(int32_t col, int log2t) {
+    return (static_cast<uint32_t>(col) * 0x9E3779B1u) >> (32 - log2t);
+}
+
+__host__ __device__ inline int ceil_log2(int64_t x) {
+    int l = 0;
+    while ((int64_t{1} << l) < x) ++l;
+    return l;
+}
+
+}  // namespace spg

@@ -1,0 +1,357 @@
+"""Python binding of the GB300 SpGEMM engine (libspgemm_gb300.so, C ABI in
+include/spgemm_gb300.h) and of the synthetic-input generators (libspg_synth.so).
+
+The engine is the only compute path: there is no CPU fallback.  Loading the
+library fails loudly when it has not been built (``python build.py`` in this
+directory, or ``__graft_entry__.build()``).
+
+Host matrices are ``Csr`` (numpy int64 row offsets, int32 columns, float64
+values, the reference's CsrMatrix layout).  Device matrices are ``DeviceCsr``
+(torch CUDA tensors of the same dtypes); torch is used only to own device
+memory.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "libspgemm_gb300.so"
+SYNTH_PATH = HERE / "libspg_synth.so"
+
+SPG_HOST, SPG_DEVICE = 0, 1
+STATUS_NAMES = {0: "SPG_OK", 1: "SPG_INVALID_ARGUMENT", 2: "SPG_OVERFLOW", 3: "SPG_OUT_OF_RANGE_COLUMN",
+                4: "SPG_OUT_OF_MEMORY", 5: "SPG_BUDGET_EXCEEDED", 6: "SPG_DEVICE_TIMEOUT", 7: "SPG_CUDA_ERROR",
+                8: "SPG_NOT_READY", 9: "SPG_CANCELLED"}
+BIN_NAMES = ["empty", "w<=32", "w<=64", "w<=128", "w<=256", "w<=512", "b<=1K", "b<=2K", "b<=4K", "b<=8K", "heavy"]
+
+
+@dataclass
+class Csr:
+    rows: int
+    cols: int
+    row_ptr: np.ndarray
+    col: np.ndarray
+    val: np.ndarray
+
+    @property
+    def nnz(self) -> int:
+        return int(self.row_ptr[-1]) if len(self.row_ptr) else 0
+
+    @staticmethod
+    def from_arrays(rows, cols, row_ptr, col, val) -> "Csr":
+        return Csr(int(rows), int(cols), np.ascontiguousarray(row_ptr, dtype=np.int64),
+                   np.ascontiguousarray(col, dtype=np.int32), np.ascontiguousarray(val, dtype=np.float64))
+
+    def to_device(self, device: int = 0) -> "DeviceCsr":
+        import torch
+        dev = torch.device("cuda", device)
+        return DeviceCsr(self.rows, self.cols, torch.from_numpy(np.ascontiguousarray(self.row_ptr)).to(dev),
+                         torch.from_numpy(np.ascontiguousarray(self.col)).to(dev),
+                         torch.from_numpy(np.ascontiguousarray(self.val)).to(dev))
+
+    def scaled(self, factor: float) -> "Csr":
+        return Csr(self.rows, self.cols, self.row_ptr.copy(), self.col.copy(), self.val * factor)
+
+
+@dataclass
+class DeviceCsr:
+    rows: int
+    cols: int
+    row_ptr: object  # torch.int64 CUDA tensor
+    col: object      # torch.int32
+    val: object      # torch.float64
+
+    @property
+    def nnz(self) -> int:
+        return int(self.col.numel())
+
+
+class SpgError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+        self.name = STATUS_NAMES.get(status, str(status))
+
+
+class _View(C.Structure):
+    _fields_ = [("rows", C.c_int32), ("cols", C.c_int32), ("nnz", C.c_int64), ("row_ptr", C.c_void_p),
+                ("col", C.c_void_p), ("val", C.c_void_p), ("location", C.c_int32)]
+
+
+class _Result(C.Structure):
+    _fields_ = [("rows", C.c_int32), ("cols", C.c_int32), ("nnz", C.c_int64), ("row_ptr", C.c_void_p),
+                ("col", C.c_void_p), ("val", C.c_void_p), ("location", C.c_int32), ("reserved", C.c_int32),
+                ("products", C.c_int64)]
+
+
+class _Config(C.Structure):
+    _fields_ = [("device", C.c_int32), ("reserved", C.c_int32), ("hbm_budget_bytes", C.c_uint64)]
+
+
+class Timings(C.Structure):
+    _fields_ = [("ms_rowwork", C.c_float), ("ms_symbolic", C.c_float), ("ms_scan", C.c_float),
+                ("ms_numeric", C.c_float), ("ms_compact", C.c_float), ("ms_total", C.c_float),
+                ("products", C.c_int64), ("nnz", C.c_int64), ("rows", C.c_int64), ("bin_rows", C.c_int64 * 11),
+                ("launches", C.c_int64)]
+
+    def as_dict(self) -> dict:
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "bin_rows"}
+        d["bin_rows"] = {BIN_NAMES[i]: int(self.bin_rows[i]) for i in range(11)}
+        return d
+
+
+class _SynthCsr(C.Structure):
+    _fields_ = [("rows", C.c_int32), ("cols", C.c_int32), ("nnz", C.c_int64),
+                ("row_ptr", C.POINTER(C.c_int64)), ("col", C.POINTER(C.c_int32)), ("val", C.POINTER(C.c_double))]
+
+
+_lib = None
+
+
+def library() -> C.CDLL:
+    """The engine library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is missing: build the CUDA engine first (python build.py)")
+        lib = C.CDLL(str(LIB_PATH), mode=os.RTLD_NOW)
+        lib.spg_last_error.restype = C.c_char_p
+        lib.spg_last_error.argtypes = [C.c_void_p]
+        lib.spg_status_string.restype = C.c_char_p
+        lib.spg_stream.restype = C.c_void_p
+        lib.spg_stream.argtypes = [C.c_void_p]
+        lib.spg_host_alloc.restype = C.c_void_p
+        lib.spg_host_alloc.argtypes = [C.c_size_t]
+        lib.spg_host_free.argtypes = [C.c_void_p]
+        lib.spg_destroy.argtypes = [C.c_void_p]
+        for name in ("spg_multiply", "spg_multiply_batch", "spg_accum_begin", "spg_accum_add", "spg_accum_finish",
+                     "spg_result_download", "spg_result_free", "spg_scalar_multiplication_count",
+                     "spg_last_timings", "spg_create", "spg_config_default"):
+            getattr(lib, name).restype = C.c_int
+        _lib = lib
+    return _lib
+
+
+def _host_view(m: Csr, keep: list) -> _View:
+    rp = np.ascontiguousarray(m.row_ptr, dtype=np.int64)
+    ci = np.ascontiguousarray(m.col, dtype=np.int32)
+    va = np.ascontiguousarray(m.val, dtype=np.float64)
+    keep += [rp, ci, va]
+    return _View(int(m.rows), int(m.cols), int(rp[-1]) if len(rp) else 0, rp.ctypes.data,
+                 ci.ctypes.data if ci.size else None, va.ctypes.data if va.size else None, SPG_HOST)
+
+
+def _dev_view(m: DeviceCsr) -> _View:
+    import torch
+    assert m.row_ptr.dtype == torch.int64 and m.col.dtype == torch.int32 and m.val.dtype == torch.float64
+    return _View(int(m.rows), int(m.cols), int(m.col.numel()), m.row_ptr.data_ptr(),
+                 m.col.data_ptr() if m.col.numel() else None, m.val.data_ptr() if m.val.numel() else None,
+                 SPG_DEVICE)
+
+
+def _view(m, keep: list) -> _View:
+    return _dev_view(m) if isinstance(m, DeviceCsr) else _host_view(m, keep)
+
+
+class DeviceResult:
+    """A result held in device memory owned by the engine."""
+
+    def __init__(self, engine: "Engine", res: _Result):
+        self._engine = engine
+        self._res = res
+        self.rows, self.cols, self.nnz, self.products = res.rows, res.cols, res.nnz, res.products
+
+    @property
+    def pointers(self) -> tuple[int, int, int]:
+        return self._res.row_ptr, self._res.col, self._res.val
+
+    def download(self) -> Csr:
+        rp = np.empty(self.rows + 1, dtype=np.int64)
+        ci = np.empty(self.nnz, dtype=np.int32)
+        va = np.empty(self.nnz, dtype=np.float64)
+        self._engine._check(library().spg_result_download(
+            self._engine.h, C.byref(self._res), rp.ctypes.data_as(C.c_void_p),
+            ci.ctypes.data_as(C.c_void_p) if self.nnz else None, va.ctypes.data_as(C.c_void_p) if self.nnz else None))
+        return Csr(self.rows, self.cols, rp, ci, va)
+
+    def free(self):
+        if self._res is not None and self._engine.h:
+            library().spg_result_free(self._engine.h, C.byref(self._res))
+        self._res = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def _take_host(res: _Result, engine: "Engine") -> Csr:
+    rows, nnz = res.rows, res.nnz
+    rp = np.ctypeslib.as_array(C.cast(res.row_ptr, C.POINTER(C.c_int64)), shape=(rows + 1,)).copy()
+    if nnz:
+        ci = np.ctypeslib.as_array(C.cast(res.col, C.POINTER(C.c_int32)), shape=(nnz,)).copy()
+        va = np.ctypeslib.as_array(C.cast(res.val, C.POINTER(C.c_double)), shape=(nnz,)).copy()
+    else:
+        ci, va = np.zeros(0, np.int32), np.zeros(0, np.float64)
+    library().spg_result_free(engine.h, C.byref(res))
+    return Csr(rows, res.cols, rp, ci, va)
+
+
+class Engine:
+    """One engine handle (one CUDA stream and its workspace) on one device."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
+        lib = library()
+        cfg = _Config(device, 0, hbm_budget_bytes)
+        h = C.c_void_p()
+        st = lib.spg_create(C.byref(cfg), C.byref(h))
+        if st != 0:
+            raise SpgError(st, "spg_create failed (no usable CUDA device?)")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            library().spg_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st: int):
+        if st != 0:
+            raise SpgError(st, library().spg_last_error(self.h).decode())
+
+    @property
+    def stream(self) -> int:
+        return library().spg_stream(self.h)
+
+    def multiply(self, a, b, out: str = "host"):
+        """C = A * B.  out="host" returns a Csr, out="device" a DeviceResult."""
+        keep: list = []
+        va, vb = _view(a, keep), _view(b, keep)
+        res = _Result()
+        loc = SPG_DEVICE if out == "device" else SPG_HOST
+        self._check(library().spg_multiply(self.h, C.byref(va), C.byref(vb), C.c_int32(loc), C.byref(res)))
+        return DeviceResult(self, res) if loc == SPG_DEVICE else _take_host(res, self)
+
+    def multiply_batch(self, pairs, out: str = "host") -> list:
+        keep: list = []
+        n = len(pairs)
+        A = (_View * max(n, 1))(*[_view(a, keep) for a, _ in pairs])
+        B = (_View * max(n, 1))(*[_view(b, keep) for _, b in pairs])
+        R = (_Result * max(n, 1))()
+        loc = SPG_DEVICE if out == "device" else SPG_HOST
+        self._check(library().spg_multiply_batch(self.h, C.c_int32(n), A, B, C.c_int32(loc), R))
+        return [DeviceResult(self, R[i]) if loc == SPG_DEVICE else _take_host(R[i], self) for i in range(n)]
+
+    def accumulate(self, rows: int, cols: int, stages, out: str = "host"):
+        """LocalAccumulator(rows, cols); addProduct(A, B) per stage; finish()."""
+        lib = library()
+        self._check(lib.spg_accum_begin(self.h, C.c_int32(rows), C.c_int32(cols)))
+        for a, b in stages:
+            keep: list = []
+            va, vb = _view(a, keep), _view(b, keep)
+            self._check(lib.spg_accum_add(self.h, C.byref(va), C.byref(vb)))
+        res = _Result()
+        loc = SPG_DEVICE if out == "device" else SPG_HOST
+        self._check(lib.spg_accum_finish(self.h, C.c_int32(loc), C.byref(res)))
+        return DeviceResult(self, res) if loc == SPG_DEVICE else _take_host(res, self)
+
+    def scalar_multiplication_count(self, a, b) -> int:
+        keep: list = []
+        va, vb = _view(a, keep), _view(b, keep)
+        n = C.c_int64()
+        self._check(library().spg_scalar_multiplication_count(self.h, C.byref(va), C.byref(vb), C.byref(n)))
+        return n.value
+
+    def last_timings(self) -> dict:
+        t = Timings()
+        self._check(library().spg_last_timings(self.h, C.byref(t)))
+        return t.as_dict()
+
+
+# ---------------------------------------------------------------------------
+# Synthetic inputs (libspg_synth.so)
+_synth = None
+
+
+def _synth_lib() -> C.CDLL:
+    global _synth
+    if _synth is None:
+        if not SYNTH_PATH.exists():
+            raise RuntimeError(f"{SYNTH_PATH} is missing: build it first (python build.py)")
+        _synth = C.CDLL(str(SYNTH_PATH), mode=os.RTLD_NOW)
+        _synth.spg_synth_powerlaw.argtypes = [C.c_int32, C.c_double, C.c_double, C.c_int32, C.c_int32, C.c_double,
+                                              C.c_uint64, C.c_void_p]
+        _synth.spg_synth_uniform.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.c_void_p]
+        _synth.spg_synth_laplacian3d.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_void_p]
+        _synth.spg_synth_restriction.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p]
+    return _synth
+
+
+def _synth_take(out: _SynthCsr) -> Csr:
+    rows, nnz = out.rows, out.nnz
+    rp = np.ctypeslib.as_array(out.row_ptr, shape=(rows + 1,)).copy()
+    ci = np.ctypeslib.as_array(out.col, shape=(max(nnz, 1),))[:nnz].copy()
+    va = np.ctypeslib.as_array(out.val, shape=(max(nnz, 1),))[:nnz].copy()
+    _synth_lib().spg_synth_free(C.byref(out))
+    return Csr(rows, out.cols, rp, ci, va)
+
+
+def synth_uniform(rows: int, cols: int, min_len: int, max_len: int | None = None, seed: int = 1) -> Csr:
+    out = _SynthCsr()
+    rc = _synth_lib().spg_synth_uniform(rows, cols, min_len, min_len if max_len is None else max_len, seed,
+                                        C.byref(out))
+    if rc:
+        raise ValueError("invalid uniform generator arguments")
+    return _synth_take(out)
+
+
+def synth_powerlaw(n: int, mean: float = 24.0, sigma: float = 1.2, max_len: int = 20000, band: int = 2048,
+                   band_frac: float = 0.7, seed: int = 1) -> Csr:
+    out = _SynthCsr()
+    if _synth_lib().spg_synth_powerlaw(n, mean, sigma, max_len, band, band_frac, seed, C.byref(out)):
+        raise ValueError("invalid power-law generator arguments")
+    return _synth_take(out)
+
+
+def synth_laplacian3d(nx: int, ny: int | None = None, nz: int | None = None) -> Csr:
+    out = _SynthCsr()
+    if _synth_lib().spg_synth_laplacian3d(nx, ny or nx, nz or nx, C.byref(out)):
+        raise ValueError("invalid grid")
+    return _synth_take(out)
+
+
+def synth_restriction(nx: int, ny: int | None = None, nz: int | None = None, transpose: bool = False) -> Csr:
+    out = _SynthCsr()
+    if _synth_lib().spg_synth_restriction(nx, ny or nx, nz or nx, int(transpose), C.byref(out)):
+        raise ValueError("invalid grid (sizes must be even)")
+    return _synth_take(out)
+
+
+def scalar_products_host(a: Csr, b: Csr) -> int:
+    """P = sum over A entries of nnz(B row) (numpy; for workload bookkeeping)."""
+    blen = np.diff(b.row_ptr)
+    return int(blen[a.col].sum()) if a.nnz else 0
+
+
+def algorithmic_bytes(a: Csr, b: Csr, products: int, c_nnz: int) -> int:
+    """Bytes a single pass must move: read A, one B row-offset pair per A entry,
+    one B entry (column + value) per product, write C."""
+    m = a.rows
+    return 8 * (m + 1) + 12 * a.nnz + 16 * a.nnz + 12 * products + 8 * (m + 1) + 12 * c_nnz
