@@ -47,12 +47,13 @@ WORKLOADS = {
 }
 
 
-def make_workload(name: str):
+def make_workload(name: str, rows: int = 0):
     """[(A, B)] host operands of the workload's products (chained products are
-    materialised once on the host)."""
+    materialised once on the host).  rows != 0 shrinks the power-law matrix
+    (profiling cases only)."""
     import spgemm_gb300 as sg
     if name == "powerlaw":
-        a = sg.synth_powerlaw(1 << 20, 24.0, 1.2, 20000, 2048, 0.7, seed=1)
+        a = sg.synth_powerlaw(rows or (1 << 20), 24.0, 1.2, 20000, 2048, 0.7, seed=1)
         return [(a, a)]
     if name == "uniform":
         return [(sg.synth_uniform(65536, 65536, 16, seed=1), sg.synth_uniform(65536, 65536, 16, seed=2))]
@@ -214,7 +215,7 @@ def cpu_sample_rows(impl, kind, a, b, threads: int, target_s: float) -> tuple[in
 def run_reference_arm(args, rank, world):
     if rank != 0:
         return
-    pairs = make_workload(args.workload)
+    pairs = make_workload(args.workload, args.rows)
     impl, kind = cpu_reference()
     threads = os.cpu_count() or 1
     per_step = max(1.0, args.reference_step_seconds)
@@ -245,7 +246,7 @@ def run_gpu_arm(args, rank, world, local):
     import torch
     import spgemm_gb300 as sg
     torch.cuda.set_device(local)
-    pairs = make_workload(args.workload)
+    pairs = make_workload(args.workload, args.rows)
     eng = sg.Engine(local)
     dev_pairs = []
     for a, b in pairs:
@@ -360,7 +361,8 @@ def run_gpu_arm(args, rank, world, local):
             "metric": "GFLOP/s", "value": value, "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": WORKLOADS[args.workload], "name": args.workload,
+            "config": {"workload": WORKLOADS[args.workload] + (f" [rows={args.rows}]" if args.rows else ""),
+                       "name": args.workload,
                        "products_per_step": int(products), "c_nnz": int(sum(c_nnz)),
                        "l2": "inputs larger than L2 (no flush)" if args.workload == "powerlaw" else
                              "inputs smaller than L2 (B stays resident between steps)",
@@ -401,6 +403,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="powerlaw")
+    ap.add_argument("--rows", type=int, default=0, help="power-law rows (default 1048576; profiling only)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--reference-step-seconds", type=float, default=8.0)
     ap.add_argument("--e2e-steps", type=int, default=5)

@@ -68,9 +68,16 @@ typedef struct {
     int64_t products;  /* scalar products of this result (FLOP count = 2 * products) */
 } spg_csr_result;
 
+/* Output layout of a multiply.  UPPER_BOUND writes every row at the prefix of
+ * its scalar-product count and compacts once (12 bytes of scratch per product,
+ * one pass over the products); EXACT first counts every row's distinct columns
+ * (a second pass over the products, no scratch); AUTO picks UPPER_BOUND unless
+ * its scratch would exceed the budget or half of the free device memory. */
+typedef enum { SPG_MODE_AUTO = 0, SPG_MODE_EXACT = 1, SPG_MODE_UPPER_BOUND = 2 } spg_mode;
+
 typedef struct {
     int32_t device;             /* CUDA device ordinal */
-    int32_t reserved;
+    int32_t mode;               /* spg_mode */
     uint64_t hbm_budget_bytes;  /* largest device footprint a request may reserve; 0 = no limit */
 } spg_config;
 
@@ -128,15 +135,17 @@ spg_status spg_last_timings(const spg_handle* handle, spg_timings* timings);
  * Replaces trident::LocalAccumulator (src/trident/common/matrix_blocks.hpp:23-32;
  * matrix_blocks.cpp:152-200): begin(rows, cols) <-> the constructor,
  * add(A, B) <-> addProduct (C += A*B, products added after the values already
- * held, each coordinate in order), finish <-> finish().  Shape mismatch
- * (A.rows != rows, B.cols != cols or A.cols != B.rows) -> SPG_INVALID_ARGUMENT
- * (matrix_blocks.cpp:155-157).  Exact zeros are absent from the result;
- * dropping them between stages does not change any result, because a later
- * stage's sum starting from +0.0 or from nothing is the same value.  One
- * accumulation per handle at a time. */
+ * held, each coordinate in order), finish <-> `finish() const` (a copy of the
+ * current sum; further add calls may follow), end releases the sum (the
+ * destructor).  Shape mismatch (A.rows != rows, B.cols != cols or
+ * A.cols != B.rows) -> SPG_INVALID_ARGUMENT (matrix_blocks.cpp:155-157).
+ * Exact zeros are absent from the result; dropping them between stages does
+ * not change any result, because a later stage's sum starting from +0.0 or
+ * from nothing is the same value.  One accumulation per handle at a time. */
 spg_status spg_accum_begin(spg_handle* handle, int32_t rows, int32_t cols);
 spg_status spg_accum_add(spg_handle* handle, const spg_csr_view* A, const spg_csr_view* B);
 spg_status spg_accum_finish(spg_handle* handle, int32_t out_location, spg_csr_result* C);
+spg_status spg_accum_end(spg_handle* handle);
 
 /* ---- batched products ------------------------------------------------------
  * n independent products C[i] = A[i] * B[i] in one set of launches per phase

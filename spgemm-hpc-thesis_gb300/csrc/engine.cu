@@ -186,6 +186,21 @@ spg_status map_err(const ErrWord& e, std::string& msg) {
     }
 }
 
+// The exact (symbolic) mode when asked for, or in auto mode when reserving
+// 12 bytes per scalar product would not fit the budget or half the free memory.
+bool use_exact_mode(spg_handle* h, int64_t products, size_t reserved) {
+    if (h->cfg.mode == SPG_MODE_EXACT) return true;
+    if (h->cfg.mode == SPG_MODE_UPPER_BOUND) return false;
+    const size_t need = static_cast<size_t>(products) * 12;
+    if (h->cfg.hbm_budget_bytes && reserved + need > h->cfg.hbm_budget_bytes) return true;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        return true;
+    }
+    return need > free_b / 2;
+}
+
 float elapsed(cudaEvent_t a, cudaEvent_t b) {
     float ms = 0;
     cudaEventElapsedTime(&ms, a, b);
@@ -269,38 +284,44 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
     for (int b = 0; b < kNumBins; ++b) bin_count[b] = static_cast<int64_t>(hc->stats.bin_count[b]);
     for (int b = 0; b <= kNumBins; ++b) bin_off[b] = hc->bin_off[b];
 
-    // heavy-row scratch shared by the symbolic and numeric phases
+    // Output layout: in the upper-bound mode every row is written at the prefix
+    // of its product count (ub) and compacted afterwards; in the exact mode a
+    // symbolic phase counts the distinct columns of every row first.
     const int64_t heavy = bin_count[kBinHeavy];
-    size_t scratch_bytes = std::max(symbolic_scratch_bytes(kBinHeavy, max_ub, heavy, h->num_sms),
-                                    numeric_scratch_bytes(kBinHeavy, max_ub, heavy, h->num_sms));
+    const bool exact = use_exact_mode(h, products, ar.bytes());
+    size_t scratch_bytes = numeric_scratch_bytes(kBinHeavy, max_ub, heavy, h->num_sms);
+    if (exact) scratch_bytes = std::max(scratch_bytes, symbolic_scratch_bytes(kBinHeavy, max_ub, heavy, h->num_sms));
     void* scratch = scratch_bytes ? ar.alloc<unsigned char>(scratch_bytes, "heavy scratch") : nullptr;
-
-    for (int b = 1; b < kNumBins; ++b) launches += bin_count[b] > 0 ? 2 : 0;  // symbolic + numeric
-    launches += 3;                                                             // scan
-    for (int b = 1; b < kNumBins; ++b)
-        launch_symbolic(b, d_jobs, items + bin_off[b], bin_count[b], max_ub, scratch, scratch_bytes, &d_ctrl->stats,
-                        &d_ctrl->err, st, h->num_sms);
-    check_cuda(cudaGetLastError(), "K2 launch");
-    cudaEventRecord(h->ev[2], st);
     int64_t* partials = ar.alloc<int64_t>(scan_partials_count(static_cast<int64_t>(slots)), "scan partials");
+    for (int b = 1; b < kNumBins; ++b) launches += bin_count[b] > 0 ? (exact ? 2 : 1) : 0;
+    launches += 3;  // scan
+    int64_t tmp_total = products;
+    if (exact) {
+        for (int b = 1; b < kNumBins; ++b)
+            launch_symbolic(b, d_jobs, items + bin_off[b], bin_count[b], max_ub, scratch, scratch_bytes,
+                            &d_ctrl->stats, &d_ctrl->err, st, h->num_sms);
+        check_cuda(cudaGetLastError(), "K2 launch");
+    }
+    cudaEventRecord(h->ev[2], st);
     launch_scan(cnt, static_cast<int64_t>(slots) - 1, partials, st);
     check_cuda(cudaGetLastError(), "K3 launch");
     cudaEventRecord(h->ev[3], st);
-    check_cuda(cudaMemcpyAsync(&hc->totals[0], cnt + slots - 1, sizeof(int64_t), cudaMemcpyDeviceToHost, st),
-               "D2H total");
-    check_cuda(cudaMemcpyAsync(&hc->err, &d_ctrl->err, sizeof(ErrWord), cudaMemcpyDeviceToHost, st), "D2H err");
-    sync(h);  // sync 2: size of C
-    if (hc->err.code) {
-        std::string msg;
-        const spg_status s = map_err(hc->err, msg);
-        throw Failure{s, msg};
+    if (exact) {
+        check_cuda(cudaMemcpyAsync(&hc->totals[0], cnt + slots - 1, sizeof(int64_t), cudaMemcpyDeviceToHost, st),
+                   "D2H total");
+        check_cuda(cudaMemcpyAsync(&hc->err, &d_ctrl->err, sizeof(ErrWord), cudaMemcpyDeviceToHost, st), "D2H err");
+        sync(h);  // exact mode: size of C
+        if (hc->err.code) {
+            std::string msg;
+            const spg_status s = map_err(hc->err, msg);
+            throw Failure{s, msg};
+        }
+        tmp_total = hc->totals[0];
     }
-    const int64_t sym_total = hc->totals[0];
-    if (h->cfg.hbm_budget_bytes &&
-        ar.bytes() + static_cast<size_t>(sym_total) * 12 > h->cfg.hbm_budget_bytes)
+    if (h->cfg.hbm_budget_bytes && ar.bytes() + static_cast<size_t>(tmp_total) * 12 > h->cfg.hbm_budget_bytes)
         throw Failure{SPG_BUDGET_EXCEEDED, "product footprint exceeds the handle's HBM budget"};
-    int32_t* c_col = ar.alloc<int32_t>(static_cast<size_t>(sym_total), "C col");
-    double* c_val = ar.alloc<double>(static_cast<size_t>(sym_total), "C val");
+    int32_t* c_col = ar.alloc<int32_t>(static_cast<size_t>(tmp_total), "C col");
+    double* c_val = ar.alloc<double>(static_cast<size_t>(tmp_total), "C val");
     for (int j = 0; j < njobs; ++j) {
         jobs[j].c_col = c_col;
         jobs[j].c_val = c_val;
@@ -312,7 +333,7 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
     check_cuda(cudaGetLastError(), "K4 launch");
     cudaEventRecord(h->ev[4], st);
     check_cuda(cudaMemcpyAsync(hc, d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, st), "D2H ctrl");
-    sync(h);  // sync 3: stored count
+    sync(h);  // stored count and errors
     if (hc->err.code) {
         std::string msg;
         const spg_status s = map_err(hc->err, msg);
@@ -322,7 +343,7 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
     int64_t* final_rp = cnt;
     int32_t* final_col = c_col;
     double* final_val = c_val;
-    if (nz_total != sym_total) {  // some sums were exact zeros: compact
+    if (nz_total != tmp_total) {  // rows with fewer entries than reserved: compact
         launch_scan(nz, static_cast<int64_t>(slots) - 1, partials, st);
         launches += 3 + njobs;
         final_col = ar.alloc<int32_t>(static_cast<size_t>(nz_total), "C col (compact)");
@@ -640,33 +661,41 @@ spg_status spg_accum_add(spg_handle* h, const spg_csr_view* A, const spg_csr_vie
     });
 }
 
+// Like the reference's `CsrMatrix finish() const`, this returns a copy of the
+// current sum and leaves the accumulation as it is (more stages may follow).
 spg_status spg_accum_finish(spg_handle* h, int32_t out_location, spg_csr_result* C) {
     return guarded(h, [&] {
         require(h->acc_active, SPG_INVALID_ARGUMENT, "no accumulation in progress");
         require(C != nullptr, SPG_INVALID_ARGUMENT, "C is NULL");
-        if (!h->acc_has) {  // no stage added: an all-empty result
-            DevResult r;
-            r.rows = h->acc_rows;
-            r.cols = h->acc_cols;
-            check_cuda(cudaMallocAsync(reinterpret_cast<void**>(&r.rp), sizeof(int64_t) * (r.rows + 1), h->stream),
-                       "alloc");
-            check_cuda(cudaMallocAsync(reinterpret_cast<void**>(&r.ci), 16, h->stream), "alloc");
-            check_cuda(cudaMallocAsync(reinterpret_cast<void**>(&r.v), 16, h->stream), "alloc");
-            check_cuda(cudaMemsetAsync(r.rp, 0, sizeof(int64_t) * (r.rows + 1), h->stream), "memset");
-            deliver(h, r, out_location, C);
-        } else {
-            DevResult r;
-            r.rows = h->acc.rows;
-            r.cols = h->acc.cols;
-            r.nnz = h->acc.nnz;
-            r.products = h->acc.products;
-            r.rp = h->acc.row_ptr;
-            r.ci = h->acc.col;
-            r.v = h->acc.val;
-            h->acc_has = false;
-            std::memset(&h->acc, 0, sizeof(h->acc));
-            deliver(h, r, out_location, C);
+        require(out_location == SPG_HOST || out_location == SPG_DEVICE, SPG_INVALID_ARGUMENT, "bad out_location");
+        DevResult r;
+        r.rows = h->acc_rows;
+        r.cols = h->acc_cols;
+        r.nnz = h->acc_has ? h->acc.nnz : 0;
+        r.products = h->acc_has ? h->acc.products : 0;
+        const size_t rp_bytes = sizeof(int64_t) * (static_cast<size_t>(r.rows) + 1);
+        check_cuda(cudaMallocAsync(reinterpret_cast<void**>(&r.rp), rp_bytes, h->stream), "alloc row_ptr");
+        check_cuda(cudaMallocAsync(reinterpret_cast<void**>(&r.ci), std::max<size_t>(16, 4 * r.nnz), h->stream),
+                   "alloc col");
+        check_cuda(cudaMallocAsync(reinterpret_cast<void**>(&r.v), std::max<size_t>(16, 8 * r.nnz), h->stream),
+                   "alloc val");
+        if (h->acc_has) {
+            check_cuda(cudaMemcpyAsync(r.rp, h->acc.row_ptr, rp_bytes, cudaMemcpyDeviceToDevice, h->stream), "D2D");
+            if (r.nnz) {
+                check_cuda(cudaMemcpyAsync(r.ci, h->acc.col, 4 * r.nnz, cudaMemcpyDeviceToDevice, h->stream), "D2D");
+                check_cuda(cudaMemcpyAsync(r.v, h->acc.val, 8 * r.nnz, cudaMemcpyDeviceToDevice, h->stream), "D2D");
+            }
+        } else {  // no stage added yet: an all-empty result
+            check_cuda(cudaMemsetAsync(r.rp, 0, rp_bytes, h->stream), "memset");
         }
+        deliver(h, r, out_location, C);
+    });
+}
+
+spg_status spg_accum_end(spg_handle* h) {
+    return guarded(h, [&] {
+        if (h->acc_has) free_result_arrays(h, &h->acc);
+        h->acc_has = false;
         h->acc_active = false;
     });
 }

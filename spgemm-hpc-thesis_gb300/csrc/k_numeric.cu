@@ -2,21 +2,23 @@
 //
 // For a row with P products the kernel
 //   1. enumerates the products in reference order (spg_enum.cuh): product t gets
-//      key = its column, seq = t, value = __dmul_rn(a, b) (one rounding, as
+//      its column, sequence number t and value __dmul_rn(a, b) (one rounding, as
 //      `const double product = aValue * b` in spgemm_exchange.cpp:287);
-//   2. sorts (key, seq) pairs by key with a stable LSD radix sort (8-bit digits,
-//      ranks from __match_any_sync and per-warp digit counters; only the bits of
-//      max(col) - min(col) are sorted), so equal columns stay in product order;
+//   2. sorts the products by column with a stable LSD radix sort (8-bit digits
+//      over the bits of max(col) - min(col) only; ranks from __match_any_sync
+//      and per-warp digit counters), so that equal columns stay in product order.
+//      When the column range and the sequence number fit in 32 bits together,
+//      the sort moves one packed word (column - min) << s | seq per product;
+//      otherwise it moves the column and a 16-bit sequence number side by side;
 //   3. sums each run of equal columns sequentially in product order with
 //      __dadd_rn, starting from its first product (the `emplace` then `+=` of
 //      spgemm_exchange.cpp:288-293), and keeps the sums that are != 0.0
 //      (spgemm_exchange.cpp:304; NaN and infinities are kept);
-//   4. writes the kept (column, sum) pairs, already in column order, at the row's
-//      offset in C_tmp and the kept count into job.nz[row].
-// The result of every coordinate is therefore bit-identical to the serial
-// reference.  Rows of <= 512 products run one per warp, rows of <= 8192 one per
-// CTA with everything in shared memory, heavier rows one per CTA with the sort
-// in a global-memory slab.
+//   4. writes the kept (column, sum) pairs, already in column order, at the
+//      row's output offset (job.cnt[row]) and the kept count into job.nz[row].
+// Every coordinate is therefore bit-identical to the serial reference.  Rows of
+// <= 512 products run one per warp, rows of <= 8192 one per CTA with everything
+// in shared memory, heavier rows one per CTA with the sort in a global slab.
 #include "spg_enum.cuh"
 
 namespace spg {
@@ -28,22 +30,23 @@ __device__ inline void row_sync() {
     else __syncthreads();
 }
 
+constexpr int log2_ceil_c(int x) { return x <= 1 ? 0 : 1 + log2_ceil_c((x + 1) / 2); }
+
 template <int W, int ITEMS>
 struct RowSmem {
     static constexpr int kCap = W * 32 * ITEMS;
-    static constexpr int kSegN = W * 32;
-    double vals[kCap];          // product values by sequence number
-    SegTab<kSegN> seg;          // enumeration batch
+    static constexpr int kSeqBits = log2_ceil_c(kCap);
+    double vals[kCap];          // product values by sequence number; run sums in place
+    SegTab<W * 32> seg;         // enumeration batch
     int64_t warp_tmp[W + 1];    // block scans
-    uint32_t keys[kCap];        // columns, sorted in place
+    uint32_t keys[kCap];        // columns (unpacked) or packed (column, sequence) words
     uint32_t hist[256 * W];     // digit counters, digit-major
     uint32_t cnt[W * ITEMS];    // kept entries per (warp, item)
-    uint16_t seqs[kCap];        // sequence numbers, permuted with keys
+    uint16_t seqs[kCap];        // sequence numbers of the unpacked path
     int32_t red[2 * W];         // min / max column reduction
 };
 
-// Exclusive scan of n uint32 counters, each of the W*32 threads owning n/(W*32)
-// consecutive counters (n = 256*W: 8 each).
+// Exclusive scan of the 256*W digit counters, 8 consecutive counters per thread.
 template <int W>
 __device__ inline void scan_counters(uint32_t* c, int64_t* tmp) {
     constexpr int kPer = 8;
@@ -57,7 +60,7 @@ __device__ inline void scan_counters(uint32_t* c, int64_t* tmp) {
         v[j] = c[tid * kPer + j];
         sum += v[j];
     }
-    uint32_t incl = warp_incl_scan(sum, lane);
+    const uint32_t incl = warp_incl_scan(sum, lane);
     uint32_t base = incl - sum;
     if (W > 1) {
         if (lane == 31) tmp[warp] = incl;
@@ -77,26 +80,51 @@ __device__ inline void scan_counters(uint32_t* c, int64_t* tmp) {
     }
 }
 
-// Stable rank of ITEMS striped items per lane against the per-warp digit
-// counters hist[d * W + warp] (which must start at zero).  rk[i] receives the
-// number of earlier items of this warp with the same digit.
+// Stable rank of one striped item against this warp's digit counters: the
+// group of lanes holding the same digit is found with __match_any_sync; its
+// first lane advances the counter by the group size (one shared atomic) and
+// broadcasts the old value.  Items of a warp are ranked in order, so ranks
+// follow (warp, item, lane) order.
+__device__ inline uint32_t rank_item(uint32_t d, uint32_t* counter_of_d, int lane) {
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const int leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter_of_d, static_cast<uint32_t>(__popc(peers)));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    return base + __popc(peers & lanemask_lt());
+}
+
+// Exclusive scan of the W*ITEMS per-(warp, item) kept counts by warp 0; the
+// total goes to red[0].
 template <int W, int ITEMS>
-__device__ inline void rank_digits(const uint32_t (&dg)[ITEMS], uint32_t (&rk)[ITEMS], uint32_t* hist, int warp) {
+__device__ inline void scan_kept(uint32_t* cnt, int32_t* red, int warp, int lane) {
+    constexpr int kN = W * ITEMS;
+    constexpr int kPer = (kN + 31) / 32;
+    if (warp == 0) {
+        uint32_t v[kPer];
+        uint32_t tot = 0;
 #pragma unroll
-    for (int i = 0; i < ITEMS; ++i) {
-        const unsigned peers = __match_any_sync(0xffffffffu, dg[i]);
-        const unsigned lt = peers & lanemask_lt();
-        const uint32_t base = hist[dg[i] * W + warp];
-        rk[i] = base + __popc(lt);
-        __syncwarp();
-        if (lt == 0) hist[dg[i] * W + warp] = base + __popc(peers);
-        __syncwarp();
+        for (int j = 0; j < kPer; ++j) {
+            const int idx = lane * kPer + j;
+            v[j] = idx < kN ? cnt[idx] : 0u;
+            tot += v[j];
+        }
+        const uint32_t incl = warp_incl_scan(tot, lane);
+        uint32_t base = incl - tot;
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            const int idx = lane * kPer + j;
+            if (idx < kN) cnt[idx] = base;
+            base += v[j];
+        }
+        if (lane == 31) red[0] = static_cast<int32_t>(incl);
     }
 }
 
 template <int W, int ITEMS>
-__device__ void numeric_row(const Job& J, int row, RowSmem<W, ITEMS>& sm) {
-    constexpr int kCap = RowSmem<W, ITEMS>::kCap;
+__device__ void numeric_row(const Job& J, int row, RowSmem<W, ITEMS>& sm, ErrWord* err) {
+    using Sm = RowSmem<W, ITEMS>;
+    constexpr int kSeqBits = Sm::kSeqBits;
     const int lane = threadIdx.x & 31;
     const int warp = W == 1 ? 0 : (threadIdx.x >> 5);
     const int tid = W == 1 ? lane : threadIdx.x;
@@ -104,16 +132,17 @@ __device__ void numeric_row(const Job& J, int row, RowSmem<W, ITEMS>& sm) {
 
     // 1. products into shared memory
     int32_t lo = INT32_MAX, hi = INT32_MIN;
-    auto put = [&](int64_t seq, const int32_t* cp, const double* vp, double sc) {
-        const int32_t c = *cp;
+    const int32_t ncols = J.B.cols;
+    team_products<W * 32, true>(J, row, sm.seg, sm.warp_tmp, tid, [&](int64_t seq, int32_t c, double b, double a) {
+        if (c < 0 || c >= ncols) {
+            raise_error(err, kErrInvalid, 4, c);
+            c = 0;
+        }
         sm.keys[seq] = static_cast<uint32_t>(c);
-        sm.seqs[seq] = static_cast<uint16_t>(seq);
-        sm.vals[seq] = __dmul_rn(sc, *vp);
+        sm.vals[seq] = __dmul_rn(a, b);
         lo = min(lo, c);
         hi = max(hi, c);
-    };
-    if (W == 1) warp_products(J, row, *reinterpret_cast<SegTab<32>*>(&sm.seg), lane, put);
-    else block_products<W * 32>(J, row, sm.seg, sm.warp_tmp, put);
+    });
     lo = warp_min(lo);
     hi = warp_max(hi);
     if (W > 1) {
@@ -132,92 +161,139 @@ __device__ void numeric_row(const Job& J, int row, RowSmem<W, ITEMS>& sm) {
     }
     row_sync<W>();
     const uint32_t cmin = static_cast<uint32_t>(lo);
-    const uint32_t range = static_cast<uint32_t>(hi - lo);
+    const uint32_t range = P ? static_cast<uint32_t>(hi - lo) : 0u;
     const int nbits = range ? 32 - __clz(range) : 0;
+    const bool packed = nbits + kSeqBits <= 32;
 
-    // 2. stable LSD radix sort of (key, seq) by key - cmin
-    for (int shift = 0; shift < nbits; shift += 8) {
-        uint32_t k[ITEMS], dg[ITEMS], rk[ITEMS];
-        uint16_t s[ITEMS];
-        for (int d = tid; d < 256 * W; d += W * 32) sm.hist[d] = 0;
-        row_sync<W>();
+    // 2. stable LSD radix sort by column
+    if (packed) {
+        // Packed words (col - cmin) << kSeqBits | seq; the first pass packs.
+        for (int shift = 0; shift < nbits || shift == 0; shift += 8) {
+            uint32_t k[ITEMS], rk[ITEMS];
+            for (int d = tid; d < 256 * W; d += W * 32) sm.hist[d] = 0;
+            row_sync<W>();
 #pragma unroll
-        for (int i = 0; i < ITEMS; ++i) {
-            const int pos = (warp * ITEMS + i) * 32 + lane;
-            const bool valid = pos < P;
-            k[i] = valid ? sm.keys[pos] : 0u;
-            s[i] = valid ? sm.seqs[pos] : uint16_t{0};
-            dg[i] = valid ? (((k[i] - cmin) >> shift) & 255u) : 255u;
-        }
-        rank_digits<W, ITEMS>(dg, rk, sm.hist, warp);
-        row_sync<W>();
-        scan_counters<W>(sm.hist, sm.warp_tmp);
-        row_sync<W>();
-#pragma unroll
-        for (int i = 0; i < ITEMS; ++i) {
-            const uint32_t dst = sm.hist[dg[i] * W + warp] + rk[i];
-            if (dst < static_cast<uint32_t>(P)) {
-                sm.keys[dst] = k[i];
-                sm.seqs[dst] = s[i];
+            for (int i = 0; i < ITEMS; ++i) {
+                const int pos = (warp * ITEMS + i) * 32 + lane;
+                uint32_t d = 255u;
+                k[i] = 0xffffffffu;
+                if (pos < P) {
+                    const uint32_t raw = sm.keys[pos];
+                    k[i] = shift == 0 ? ((raw - cmin) << kSeqBits) | static_cast<uint32_t>(pos) : raw;
+                    d = (k[i] >> (kSeqBits + shift)) & 255u;
+                }
+                rk[i] = rank_item(d, &sm.hist[d * W + warp], lane);
             }
+            if (nbits == 0) {  // one column: already in sequence order; just pack
+                row_sync<W>();
+#pragma unroll
+                for (int i = 0; i < ITEMS; ++i) {
+                    const int pos = (warp * ITEMS + i) * 32 + lane;
+                    if (pos < P) sm.keys[pos] = k[i];
+                }
+                row_sync<W>();
+                break;
+            }
+            row_sync<W>();
+            scan_counters<W>(sm.hist, sm.warp_tmp);
+            row_sync<W>();
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) {
+                // Padding items were ranked under digit 255; a recomputed digit of
+                // 0xffffffff is not 255 once fewer than 8 key bits remain.
+                const int pos = (warp * ITEMS + i) * 32 + lane;
+                if (pos < P) {
+                    const uint32_t d = (k[i] >> (kSeqBits + shift)) & 255u;
+                    sm.keys[sm.hist[d * W + warp] + rk[i]] = k[i];
+                }
+            }
+            row_sync<W>();
         }
+    } else {
+        for (int i = tid; i < P; i += W * 32) sm.seqs[i] = static_cast<uint16_t>(i);
         row_sync<W>();
+        for (int shift = 0; shift < nbits; shift += 8) {
+            uint32_t k[ITEMS], rk[ITEMS];
+            uint16_t s[ITEMS];
+            for (int d = tid; d < 256 * W; d += W * 32) sm.hist[d] = 0;
+            row_sync<W>();
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) {
+                const int pos = (warp * ITEMS + i) * 32 + lane;
+                const bool valid = pos < P;
+                k[i] = valid ? sm.keys[pos] : 0u;
+                s[i] = valid ? sm.seqs[pos] : uint16_t{0};
+                const uint32_t d = valid ? (((k[i] - cmin) >> shift) & 255u) : 255u;
+                rk[i] = rank_item(d, &sm.hist[d * W + warp], lane);
+            }
+            row_sync<W>();
+            scan_counters<W>(sm.hist, sm.warp_tmp);
+            row_sync<W>();
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) {
+                const int pos = (warp * ITEMS + i) * 32 + lane;
+                const uint32_t d = pos < P ? (((k[i] - cmin) >> shift) & 255u) : 255u;
+                const uint32_t dst = sm.hist[d * W + warp] + rk[i];
+                if (dst < static_cast<uint32_t>(P)) {
+                    sm.keys[dst] = k[i];
+                    sm.seqs[dst] = s[i];
+                }
+            }
+            row_sync<W>();
+        }
     }
 
-    // 3. runs of equal columns, summed in product order
-    double sum[ITEMS];
-    uint32_t col[ITEMS];
-    unsigned keepmask[ITEMS];
+    // Column and sequence number of sorted position pos.
+    auto col_at = [&](int pos) -> uint32_t {
+        return packed ? (sm.keys[pos] >> kSeqBits) : sm.keys[pos] - cmin;
+    };
+    auto seq_at = [&](int pos) -> uint32_t {
+        return packed ? (sm.keys[pos] & ((1u << kSeqBits) - 1u)) : sm.seqs[pos];
+    };
+
+    // 3. runs of equal columns summed in product order; each run's sum is stored
+    //    in place of its first product's value
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i) {
         const int pos = (warp * ITEMS + i) * 32 + lane;
         bool keep = false;
-        sum[i] = 0.0;
-        col[i] = 0;
         if (pos < P) {
-            const uint32_t key = sm.keys[pos];
-            if (pos == 0 || sm.keys[pos - 1] != key) {
-                double acc = sm.vals[sm.seqs[pos]];
-                for (int q = pos + 1; q < P && sm.keys[q] == key; ++q) acc = __dadd_rn(acc, sm.vals[sm.seqs[q]]);
-                sum[i] = acc;
-                col[i] = key;
+            const uint32_t c = col_at(pos);
+            if (pos == 0 || col_at(pos - 1) != c) {
+                const uint32_t s0 = seq_at(pos);
+                double acc = sm.vals[s0];
+                for (int q = pos + 1; q < P && col_at(q) == c; ++q) acc = __dadd_rn(acc, sm.vals[seq_at(q)]);
+                sm.vals[s0] = acc;
                 keep = acc != 0.0;
             }
         }
-        keepmask[i] = __ballot_sync(0xffffffffu, keep);
-        if (lane == 0) sm.cnt[warp * ITEMS + i] = __popc(keepmask[i]);
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (lane == 0) sm.cnt[warp * ITEMS + i] = __popc(m);
     }
     row_sync<W>();
-    // exclusive scan of the W*ITEMS kept counts by warp 0
-    constexpr int kN = W * ITEMS;
-    constexpr int kPer = (kN + 31) / 32;
-    if (warp == 0) {
-        uint32_t v[kPer];
-        uint32_t tot = 0;
-#pragma unroll
-        for (int j = 0; j < kPer; ++j) {
-            const int idx = lane * kPer + j;
-            v[j] = idx < kN ? sm.cnt[idx] : 0u;
-            tot += v[j];
-        }
-        const uint32_t incl = warp_incl_scan(tot, lane);
-        uint32_t base = incl - tot;
-#pragma unroll
-        for (int j = 0; j < kPer; ++j) {
-            const int idx = lane * kPer + j;
-            if (idx < kN) sm.cnt[idx] = base;
-            base += v[j];
-        }
-        if (lane == 31) sm.red[0] = static_cast<int32_t>(incl);
-    }
+    scan_kept<W, ITEMS>(sm.cnt, sm.red, warp, lane);
     row_sync<W>();
+
+    // 4. kept (column, sum) pairs in sorted order
     const int64_t out0 = J.cnt[row];
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i) {
-        if (keepmask[i] & (1u << lane)) {
-            const int64_t idx = out0 + sm.cnt[warp * ITEMS + i] + __popc(keepmask[i] & lanemask_lt());
-            J.c_col[idx] = static_cast<int32_t>(col[i]);
-            J.c_val[idx] = sum[i];
+        const int pos = (warp * ITEMS + i) * 32 + lane;
+        bool keep = false;
+        uint32_t c = 0;
+        double v = 0.0;
+        if (pos < P) {
+            c = col_at(pos);
+            if (pos == 0 || col_at(pos - 1) != c) {
+                v = sm.vals[seq_at(pos)];
+                keep = v != 0.0;
+            }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (keep) {
+            const int64_t idx = out0 + sm.cnt[warp * ITEMS + i] + __popc(m & lanemask_lt());
+            J.c_col[idx] = static_cast<int32_t>(c + cmin);
+            J.c_val[idx] = v;
         }
     }
     if (tid == 0) J.nz[row] = sm.red[0];
@@ -229,7 +305,7 @@ constexpr int kWarpKernelThreads = 256;
 template <int ITEMS>
 __global__ void __launch_bounds__(kWarpKernelThreads)
 num_warp_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items, int64_t count,
-                Stats* __restrict__ stats) {
+                Stats* __restrict__ stats, ErrWord* __restrict__ err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     using Sm = RowSmem<1, ITEMS>;
     Sm& sm = reinterpret_cast<Sm*>(smem_raw)[threadIdx.x >> 5];
@@ -243,7 +319,7 @@ num_warp_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items,
         const int64_t it = items[i];
         const Job& J = jobs[item_job(it)];
         const int row = item_row(it);
-        numeric_row<1, ITEMS>(J, row, sm);
+        numeric_row<1, ITEMS>(J, row, sm, err);
         if ((threadIdx.x & 31) == 0) mine += static_cast<unsigned long long>(J.nz[row]);
     }
     if ((threadIdx.x & 31) == 0 && mine) atomicAdd(&s_nz, mine);
@@ -251,10 +327,10 @@ num_warp_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items,
     if (threadIdx.x == 0 && s_nz) atomicAdd(&stats->nz_total, s_nz);
 }
 
-template <int W, int ITEMS>
-__global__ void __launch_bounds__(W * 32)
+template <int W, int ITEMS, int MINB>
+__global__ void __launch_bounds__(W * 32, MINB)
 num_block_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items, int64_t count,
-                 Stats* __restrict__ stats) {
+                 Stats* __restrict__ stats, ErrWord* __restrict__ err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     using Sm = RowSmem<W, ITEMS>;
     Sm& sm = *reinterpret_cast<Sm*>(smem_raw);
@@ -263,7 +339,7 @@ num_block_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items
         const int64_t it = items[i];
         const Job& J = jobs[item_job(it)];
         const int row = item_row(it);
-        numeric_row<W, ITEMS>(J, row, sm);
+        numeric_row<W, ITEMS>(J, row, sm, err);
         if (threadIdx.x == 0) mine += static_cast<unsigned long long>(J.nz[row]);
     }
     if (threadIdx.x == 0 && mine) atomicAdd(&stats->nz_total, mine);
@@ -307,7 +383,7 @@ __device__ inline HeavySlab heavy_slab(void* base, int64_t cap, int cta) {
 
 __global__ void __launch_bounds__(kHeavyThreads)
 num_heavy_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items, int64_t count, void* slabs,
-                 int64_t cap, Stats* __restrict__ stats) {
+                 int64_t cap, Stats* __restrict__ stats, ErrWord* __restrict__ err) {
     __shared__ HeavySmem sm;
     const HeavySlab sl = heavy_slab(slabs, cap, blockIdx.x);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, tid = threadIdx.x;
@@ -317,14 +393,18 @@ num_heavy_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items
         const Job& J = jobs[item_job(it)];
         const int row = item_row(it);
         const int64_t P = J.ub[row];
+        const int32_t ncols = J.B.cols;
 
         int32_t lo = INT32_MAX, hi = INT32_MIN;
-        block_products<kHeavyThreads>(J, row, sm.seg, sm.warp_tmp,
-                                      [&](int64_t seq, const int32_t* cp, const double* vp, double sc) {
-            const int32_t c = *cp;
+        team_products<kHeavyThreads, true>(J, row, sm.seg, sm.warp_tmp, tid,
+                                           [&](int64_t seq, int32_t c, double b, double a) {
+            if (c < 0 || c >= ncols) {
+                raise_error(err, kErrInvalid, 4, c);
+                c = 0;
+            }
             sl.keys[0][seq] = static_cast<uint32_t>(c);
             sl.seqs[0][seq] = static_cast<uint32_t>(seq);
-            sl.vals[seq] = __dmul_rn(sc, *vp);
+            sl.vals[seq] = __dmul_rn(a, b);
             lo = min(lo, c);
             hi = max(hi, c);
         });
@@ -376,7 +456,7 @@ num_heavy_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items
             __syncthreads();
             for (int64_t t = 0; t < ntiles; ++t) {
                 const int64_t tile0 = t * kHeavyTile;
-                uint32_t k[kHeavyItems], s[kHeavyItems], dg[kHeavyItems], rk[kHeavyItems];
+                uint32_t k[kHeavyItems], s[kHeavyItems], rk[kHeavyItems];
                 for (int d = tid; d < 256 * kHeavyW; d += kHeavyThreads) sm.hist[d] = 0;
                 __syncthreads();
 #pragma unroll
@@ -385,11 +465,11 @@ num_heavy_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items
                     const bool valid = pos < P;
                     k[i] = valid ? kin[pos] : 0u;
                     s[i] = valid ? sin[pos] : 0u;
-                    dg[i] = valid ? (((k[i] - cmin) >> shift) & 255u) : 255u;
+                    const uint32_t d = valid ? (((k[i] - cmin) >> shift) & 255u) : 255u;
+                    rk[i] = rank_item(d, &sm.hist[d * kHeavyW + warp], lane);
                 }
-                rank_digits<kHeavyW, kHeavyItems>(dg, rk, sm.hist, warp);
                 __syncthreads();
-                if (tid < 256) {  // this tile's count of digit tid (padding included)
+                if (tid < 256) {  // this tile's count of digit tid
                     uint32_t c = 0;
 #pragma unroll
                     for (int w = 0; w < kHeavyW; ++w) c += sm.hist[tid * kHeavyW + w];
@@ -402,16 +482,16 @@ num_heavy_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items
                 for (int i = 0; i < kHeavyItems; ++i) {
                     const int64_t pos = tile0 + (warp * kHeavyItems + i) * 32 + lane;
                     if (pos < P) {
-                        // within-tile position of this item among its digit, then the row-wide base
-                        const uint32_t within = sm.hist[dg[i] * kHeavyW + warp] + rk[i] - sm.hist[dg[i] * kHeavyW];
-                        const uint32_t dst = sm.digit_base[dg[i]] + within;
+                        const uint32_t d = ((k[i] - cmin) >> shift) & 255u;
+                        // position among this tile's items of digit d, then the row-wide base
+                        const uint32_t within = sm.hist[d * kHeavyW + warp] + rk[i] - sm.hist[d * kHeavyW];
+                        const uint32_t dst = sm.digit_base[d] + within;
                         kout[dst] = k[i];
                         sout[dst] = s[i];
                     }
                 }
                 __syncthreads();
-                if (tid < 256) sm.digit_base[tid] += sm.digit_tot[tid] - (tid == 255 ? static_cast<uint32_t>(
-                    (tile0 + kHeavyTile > P) ? (tile0 + kHeavyTile - P) : 0) : 0u);
+                if (tid < 256) sm.digit_base[tid] += sm.digit_tot[tid];
                 __syncthreads();
             }
             cur ^= 1;
@@ -448,22 +528,7 @@ num_heavy_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items
                 if (lane == 0) sm.cnt[warp * kHeavyItems + i] = __popc(keepmask[i]);
             }
             __syncthreads();
-            if (warp == 0) {  // 256 counts, 8 per lane
-                uint32_t v[8], tot = 0;
-#pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    v[j] = sm.cnt[lane * 8 + j];
-                    tot += v[j];
-                }
-                const uint32_t incl = warp_incl_scan(tot, lane);
-                uint32_t base = incl - tot;
-#pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    sm.cnt[lane * 8 + j] = base;
-                    base += v[j];
-                }
-                if (lane == 31) sm.red[0] = static_cast<int32_t>(incl);
-            }
+            scan_kept<kHeavyW, kHeavyItems>(sm.cnt, sm.red, warp, lane);
             __syncthreads();
             const int64_t tile_out = out0 + sm.out_base;
 #pragma unroll
@@ -495,17 +560,21 @@ int capped(int64_t work, int per_block, int cap) {
 int heavy_grid(int64_t count, int num_sms) { return static_cast<int>(count < num_sms ? count : num_sms); }
 
 template <int ITEMS>
-void run_warp(const Job* jobs, const int64_t* items, int64_t count, Stats* stats, cudaStream_t st, int num_sms) {
+void run_warp(const Job* jobs, const int64_t* items, int64_t count, Stats* stats, ErrWord* err, cudaStream_t st,
+              int num_sms) {
     const int smem = 8 * static_cast<int>(sizeof(RowSmem<1, ITEMS>));
     cudaFuncSetAttribute(num_warp_kernel<ITEMS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    num_warp_kernel<ITEMS><<<capped(count, 8, num_sms * 16), kWarpKernelThreads, smem, st>>>(jobs, items, count, stats);
+    num_warp_kernel<ITEMS><<<capped(count, 8, num_sms * 16), kWarpKernelThreads, smem, st>>>(jobs, items, count, stats,
+                                                                                           err);
 }
 
-template <int W, int ITEMS>
-void run_block(const Job* jobs, const int64_t* items, int64_t count, Stats* stats, cudaStream_t st, int num_sms) {
+template <int W, int ITEMS, int MINB>
+void run_block(const Job* jobs, const int64_t* items, int64_t count, Stats* stats, ErrWord* err, cudaStream_t st,
+               int num_sms) {
     const int smem = static_cast<int>(sizeof(RowSmem<W, ITEMS>));
-    cudaFuncSetAttribute(num_block_kernel<W, ITEMS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    num_block_kernel<W, ITEMS><<<capped(count, 1, num_sms * 8), W * 32, smem, st>>>(jobs, items, count, stats);
+    cudaFuncSetAttribute(num_block_kernel<W, ITEMS, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    num_block_kernel<W, ITEMS, MINB><<<capped(count, 1, num_sms * 8), W * 32, smem, st>>>(jobs, items, count, stats,
+                                                                                         err);
 }
 
 }  // namespace
@@ -516,21 +585,21 @@ size_t numeric_scratch_bytes(int bin, int64_t max_ub, int64_t count, int num_sms
 }
 
 void launch_numeric(int bin, const Job* d_jobs, const int64_t* d_items, int64_t count, int64_t max_ub,
-                    void* d_scratch, size_t, Stats* d_stats, ErrWord*, cudaStream_t st, int num_sms) {
+                    void* d_scratch, size_t, Stats* d_stats, ErrWord* d_err, cudaStream_t st, int num_sms) {
     if (count <= 0) return;
     switch (bin) {
-        case kBinW1: run_warp<1>(d_jobs, d_items, count, d_stats, st, num_sms); break;
-        case kBinW2: run_warp<2>(d_jobs, d_items, count, d_stats, st, num_sms); break;
-        case kBinW4: run_warp<4>(d_jobs, d_items, count, d_stats, st, num_sms); break;
-        case kBinW8: run_warp<8>(d_jobs, d_items, count, d_stats, st, num_sms); break;
-        case kBinW16: run_warp<16>(d_jobs, d_items, count, d_stats, st, num_sms); break;
-        case kBinB1K: run_block<4, 8>(d_jobs, d_items, count, d_stats, st, num_sms); break;
-        case kBinB2K: run_block<8, 8>(d_jobs, d_items, count, d_stats, st, num_sms); break;
-        case kBinB4K: run_block<8, 16>(d_jobs, d_items, count, d_stats, st, num_sms); break;
-        case kBinB8K: run_block<16, 16>(d_jobs, d_items, count, d_stats, st, num_sms); break;
+        case kBinW1: run_warp<1>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;
+        case kBinW2: run_warp<2>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;
+        case kBinW4: run_warp<4>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;
+        case kBinW8: run_warp<8>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;
+        case kBinW16: run_warp<16>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;
+        case kBinB1K: run_block<4, 8, 6>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;
+        case kBinB2K: run_block<8, 8, 3>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;
+        case kBinB4K: run_block<8, 16, 2>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;
+        case kBinB8K: run_block<16, 16, 1>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;
         case kBinHeavy:
             num_heavy_kernel<<<heavy_grid(count, num_sms), kHeavyThreads, 0, st>>>(d_jobs, d_items, count, d_scratch,
-                                                                                   max_ub, d_stats);
+                                                                                   max_ub, d_stats, d_err);
             break;
         default: break;
     }

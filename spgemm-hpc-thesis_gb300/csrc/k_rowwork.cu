@@ -66,10 +66,7 @@ rowwork_kernel(const Job* __restrict__ jobs, int njobs, const int64_t* __restric
             if (bad_row) raise_error(err, kErrInvalid, 3, row);
             if (J.S.rp) len += J.S.rp[row + 1] - J.S.rp[row];
             J.ub[row] = len;
-            if (len == 0) {
-                J.cnt[row] = 0;
-                J.nz[row] = 0;
-            }
+            J.cnt[row] = len;  // upper-bound layout; the exact mode's symbolic phase overwrites it
             atomicAdd(&s_bins[bin_of(len)], 1ull);
             atomicAdd(&s_products, static_cast<unsigned long long>(len));
             atomicMax(&s_max, static_cast<unsigned long long>(len));

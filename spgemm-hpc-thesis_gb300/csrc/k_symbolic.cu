@@ -56,8 +56,8 @@ sym_warp_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items,
         if (tiny) {
             // <= 32 products: product t goes to lane t; count the first lane of each column group.
             int32_t* stage = s_tab[w];
-            warp_products(J, row, s_seg[w], lane, [&](int64_t seq, const int32_t* cp, const double*, double) {
-                stage[seq] = *cp;
+            team_products<32, false>(J, row, s_seg[w], nullptr, lane, [&](int64_t seq, int32_t c, double, double) {
+                stage[seq] = c;
             });
             __syncwarp();
             const bool valid = lane < ub;
@@ -74,8 +74,7 @@ sym_warp_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items,
             for (uint32_t s = lane; s < tsize; s += 32) tab[s] = -1;
             __syncwarp();
             int mine = 0;
-            warp_products(J, row, s_seg[w], lane, [&](int64_t, const int32_t* cp, const double*, double) {
-                const int32_t c = *cp;
+            team_products<32, false>(J, row, s_seg[w], nullptr, lane, [&](int64_t, int32_t c, double, double) {
                 if (col_ok(c, J.B.cols, err)) mine += hash_insert(tab, mask, log2t, c);
             });
             found = warp_sum(mine);
@@ -102,9 +101,8 @@ sym_block_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items
         if (threadIdx.x == 0) s_found = 0;
         __syncthreads();
         int mine = 0;
-        block_products<kSymBlockThreads>(J, row, s_seg, s_warp,
-                                         [&](int64_t, const int32_t* cp, const double*, double) {
-            const int32_t c = *cp;
+        team_products<kSymBlockThreads, false>(J, row, s_seg, s_warp, threadIdx.x,
+                                               [&](int64_t, int32_t c, double, double) {
             if (col_ok(c, J.B.cols, err)) mine += hash_insert(s_tab, mask, log2t, c);
         });
         mine = warp_sum(mine);
@@ -132,9 +130,8 @@ sym_heavy_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items
         if (threadIdx.x == 0) s_found = 0;
         __syncthreads();
         int mine = 0;
-        block_products<kSymHeavyThreads>(J, row, s_seg, s_warp,
-                                         [&](int64_t, const int32_t* cp, const double*, double) {
-            const int32_t c = *cp;
+        team_products<kSymHeavyThreads, false>(J, row, s_seg, s_warp, threadIdx.x,
+                                               [&](int64_t, int32_t c, double, double) {
             if (col_ok(c, J.B.cols, err)) mine += hash_insert(tab, mask, log2t, c);
         });
         mine = warp_sum(mine);

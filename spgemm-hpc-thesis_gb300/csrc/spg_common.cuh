@@ -31,7 +31,8 @@ struct CsrView {
 struct Job {
     CsrView A, B, S;          // S.rp == nullptr: no addend
     int64_t* ub = nullptr;    // [A.rows]  products per row (upper bound of its nnz)
-    int64_t* cnt = nullptr;   // [A.rows+1] distinct columns per row, scanned in place into C_tmp offsets
+    int64_t* cnt = nullptr;   // [A.rows+1] reserved entries per row (ub, or distinct columns in the
+                              // exact mode), scanned in place into C_tmp offsets
     int64_t* nz = nullptr;    // [A.rows+1] stored (nonzero) entries per row
     int32_t* c_col = nullptr; // C_tmp columns (size = total of cnt)
     double* c_val = nullptr;  // C_tmp values

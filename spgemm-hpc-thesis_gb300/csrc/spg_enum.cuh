@@ -8,9 +8,12 @@
 // 279-294) visit them.
 //
 // Segments are processed in batches of one per thread: the batch's segment
-// lengths are scanned, their descriptors are staged in shared memory, and the
-// threads then stride over the batch's products, so that neighbouring threads
-// read neighbouring B entries (coalesced) whatever the segment lengths are.
+// lengths are scanned and its descriptors staged in shared memory.  The team's
+// threads then stride over the batch's products (neighbouring threads read
+// neighbouring B entries, coalesced), four products per thread at a time: each
+// of the four finds its segment by binary search, then the four column and four
+// value loads are issued together, so a thread keeps eight independent global
+// loads in flight instead of one.
 #pragma once
 
 #include "spg_common.cuh"
@@ -55,42 +58,6 @@ __device__ inline int seg_search(const int64_t* incl, int64_t t) {
     return j;
 }
 
-// Warp-cooperative enumeration.  f(seq, colp, valp, scale) is called once per
-// product by the lane that owns it; lanes own products t = lane, lane+32, ...
-// of each batch.  All 32 lanes must call this together.
-template <typename F>
-__device__ inline void warp_products(const Job& J, int row, SegTab<32>& tab, int lane, F&& f) {
-    const bool has_s = J.S.rp != nullptr;
-    const int64_t a0 = J.A.rp[row];
-    const int64_t nseg = (J.A.rp[row + 1] - a0) + (has_s ? 1 : 0);
-    int64_t seq_base = 0;
-    for (int64_t e0 = 0; e0 < nseg; e0 += 32) {
-        const int64_t e = e0 + lane;
-        const int32_t* cp = nullptr;
-        const double* vp = nullptr;
-        double sc = 1.0;
-        int64_t len = 0;
-        if (e < nseg) row_segment(J, row, a0, has_s, e, cp, vp, sc, len);
-        const int64_t incl = warp_incl_scan(len, lane);
-        tab.colp[lane] = cp;
-        tab.valp[lane] = vp;
-        tab.scale[lane] = sc;
-        tab.incl[lane] = incl;
-        __syncwarp();
-        const int64_t total = tab.incl[31];
-        if (lane < total) {
-            int j = seg_search<32>(tab.incl, lane);
-            for (int64_t t = lane; t < total; t += 32) {
-                while (tab.incl[j] <= t) ++j;
-                const int64_t q = t - (j ? tab.incl[j - 1] : 0);
-                f(seq_base + t, tab.colp[j] + q, tab.valp[j] + q, tab.scale[j]);
-            }
-        }
-        seq_base += total;
-        __syncwarp();
-    }
-}
-
 // Inclusive block scan of int64 (NT threads, NT/32 <= 32 warps).
 template <int NT>
 __device__ inline int64_t block_incl_scan(int64_t v, int64_t* s_warp /* NT/32 + 1 */) {
@@ -110,11 +77,19 @@ __device__ inline int64_t block_incl_scan(int64_t v, int64_t* s_warp /* NT/32 + 
     return out;
 }
 
-// Block-cooperative enumeration (all NT threads call it together).  Threads
-// own products t = tid, tid+NT, ... of each batch of NT segments.
-template <int NT, typename F>
-__device__ inline void block_products(const Job& J, int row, SegTab<NT>& tab, int64_t* s_warp, F&& f) {
-    const int tid = threadIdx.x;
+template <int NT>
+__device__ inline void team_sync() {
+    if (NT == 32) __syncwarp();
+    else __syncthreads();
+}
+
+// Team-cooperative enumeration: a warp (NT == 32, tid = lane) or a whole CTA
+// (NT == blockDim.x, tid = threadIdx.x); every thread of the team must call it.
+// f(seq, col, b, a) is called once per product by the thread that owns it, with
+// the B entry's column `col`, its value `b` and the scale `a` (the product is
+// a*b).  kLoadVal = false skips the value loads (b is then 0).
+template <int NT, bool kLoadVal, typename F>
+__device__ inline void team_products(const Job& J, int row, SegTab<NT>& tab, int64_t* s_warp, int tid, F&& f) {
     const bool has_s = J.S.rp != nullptr;
     const int64_t a0 = J.A.rp[row];
     const int64_t nseg = (J.A.rp[row + 1] - a0) + (has_s ? 1 : 0);
@@ -126,23 +101,38 @@ __device__ inline void block_products(const Job& J, int row, SegTab<NT>& tab, in
         double sc = 1.0;
         int64_t len = 0;
         if (e < nseg) row_segment(J, row, a0, has_s, e, cp, vp, sc, len);
-        const int64_t incl = block_incl_scan<NT>(len, s_warp);
+        int64_t incl;
+        if constexpr (NT == 32) incl = warp_incl_scan(len, tid);
+        else incl = block_incl_scan<NT>(len, s_warp);
         tab.colp[tid] = cp;
         tab.valp[tid] = vp;
         tab.scale[tid] = sc;
         tab.incl[tid] = incl;
-        __syncthreads();
+        team_sync<NT>();
         const int64_t total = tab.incl[NT - 1];
-        if (tid < total) {
-            int j = seg_search<NT>(tab.incl, tid);
-            for (int64_t t = tid; t < total; t += NT) {
-                while (tab.incl[j] <= t) ++j;
-                const int64_t q = t - (j ? tab.incl[j - 1] : 0);
-                f(seq_base + t, tab.colp[j] + q, tab.valp[j] + q, tab.scale[j]);
+        for (int64_t t0 = tid; t0 < total; t0 += 4 * NT) {
+            int j[4];
+            int64_t q[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int64_t t = t0 + u * NT;
+                j[u] = t < total ? seg_search<NT>(tab.incl, t) : 0;
+                q[u] = t < total ? t - (j[u] ? tab.incl[j[u] - 1] : 0) : 0;
             }
+            int32_t c[4];
+            double b[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const bool ok = t0 + u * NT < total;
+                c[u] = ok ? __ldg(tab.colp[j[u]] + q[u]) : 0;
+                b[u] = (kLoadVal && ok) ? __ldg(tab.valp[j[u]] + q[u]) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (t0 + u * NT < total) f(seq_base + t0 + u * NT, c[u], b[u], tab.scale[j[u]]);
         }
         seq_base += total;
-        __syncthreads();
+        team_sync<NT>();
     }
 }
 

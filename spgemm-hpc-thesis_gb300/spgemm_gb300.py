@@ -90,7 +90,10 @@ class _Result(C.Structure):
 
 
 class _Config(C.Structure):
-    _fields_ = [("device", C.c_int32), ("reserved", C.c_int32), ("hbm_budget_bytes", C.c_uint64)]
+    _fields_ = [("device", C.c_int32), ("mode", C.c_int32), ("hbm_budget_bytes", C.c_uint64)]
+
+
+MODES = {"auto": 0, "exact": 1, "upper_bound": 2}
 
 
 class Timings(C.Structure):
@@ -206,9 +209,9 @@ def _take_host(res: _Result, engine: "Engine") -> Csr:
 class Engine:
     """One engine handle (one CUDA stream and its workspace) on one device."""
 
-    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0, mode: str = "auto"):
         lib = library()
-        cfg = _Config(device, 0, hbm_budget_bytes)
+        cfg = _Config(device, MODES[mode], hbm_budget_bytes)
         h = C.c_void_p()
         st = lib.spg_create(C.byref(cfg), C.byref(h))
         if st != 0:
@@ -270,6 +273,7 @@ class Engine:
         res = _Result()
         loc = SPG_DEVICE if out == "device" else SPG_HOST
         self._check(lib.spg_accum_finish(self.h, C.c_int32(loc), C.byref(res)))
+        self._check(lib.spg_accum_end(self.h))
         return DeviceResult(self, res) if loc == SPG_DEVICE else _take_host(res, self)
 
     def scalar_multiplication_count(self, a, b) -> int:

@@ -1,0 +1,88 @@
+// The C++ drop-in layer (include/spgemm_gb300.hpp) used the way the reference's
+// host code uses its multiply: with the reference's CsrMatrix layout, its
+// known answers (spgemm_serial_smoke.cpp:65-67, spgemm_validation_smoke.cpp:
+// 153-155, trident_accumulator_memory.cpp:40-60) and its exception types.
+#include <cstdio>
+#include <stdexcept>
+#include <vector>
+
+#include "spgemm_gb300.hpp"
+
+struct CsrMatrix {  // the layout of src/common/csr_matrix.hpp:43-49
+    int rows = 0;
+    int cols = 0;
+    std::vector<int64_t> rowPtr;
+    std::vector<int> columnIndices;
+    std::vector<double> values;
+};
+
+#define REQUIRE(x)                                                   \
+    do {                                                             \
+        if (!(x)) {                                                  \
+            std::fprintf(stderr, "FAILED: %s (line %d)\n", #x, __LINE__); \
+            return 1;                                                \
+        }                                                            \
+    } while (0)
+
+int main() {
+    namespace g = spgemm_gb300;
+    const CsrMatrix a{2, 3, {0, 2, 3}, {0, 2, 1}, {1.0, 2.0, 3.0}};
+    const CsrMatrix b{3, 2, {0, 1, 2, 3}, {1, 0, 1}, {4.0, 5.0, 6.0}};
+    const CsrMatrix c = g::spgemm(a, b);
+    REQUIRE(c.rows == 2 && c.cols == 2 && c.rowPtr == (std::vector<int64_t>{0, 1, 2}));
+    REQUIRE(c.columnIndices == (std::vector<int>{1, 0}) && c.values == (std::vector<double>{16.0, 15.0}));
+    REQUIRE(g::thread_engine().scalarMultiplicationCount(a, b) == 3);
+
+    const CsrMatrix ca{3, 2, {0, 2, 2, 3}, {0, 1, 1}, {1, 1, 2}};
+    const CsrMatrix cb{2, 3, {0, 2, 4}, {0, 1, 0, 2}, {1, 2, -1, 3}};
+    const CsrMatrix cc = g::spgemm(ca, cb);
+    REQUIRE(cc.rowPtr == (std::vector<int64_t>{0, 2, 2, 4}));
+    REQUIRE(cc.columnIndices == (std::vector<int>{1, 2, 0, 2}) && cc.values == (std::vector<double>{2, 3, -2, 6}));
+
+    bool caught = false;
+    try {
+        g::spgemm(a, a);  // 2x3 * 2x3
+    } catch (const std::invalid_argument&) {
+        caught = true;
+    }
+    REQUIRE(caught);
+    caught = false;
+    try {
+        const CsrMatrix bad{1, 2, {0, 1}, {5}, {1.0}};
+        const CsrMatrix two{2, 2, {0, 1, 2}, {0, 1}, {1.0, 1.0}};
+        g::spgemm(bad, two);
+    } catch (const std::runtime_error&) {
+        caught = true;
+    }
+    REQUIRE(caught);
+
+    // three stages with cross-stage cancellation and an empty row
+    CsrMatrix sa{3, 2, {0, 3, 3, 4}, {1, 0, 1, 0}, {2.0, 1.0, -1.0, 3.0}};
+    const CsrMatrix sb{2, 4, {0, 3, 5}, {3, 1, 3, 0, 1}, {2.0, 4.0, -1.0, 5.0, -4.0}};
+    {
+        g::LocalAccumulator<CsrMatrix> acc(3, 4);
+        acc.addProduct(sa, sb);
+        for (auto& v : sa.values) v *= -1.0;
+        acc.addProduct(sa, sb);
+        for (auto& v : sa.values) v *= -0.5;
+        acc.addProduct(sa, sb);
+        const CsrMatrix r1 = acc.finish();
+        const CsrMatrix r2 = acc.finish();  // finish() is const: same result twice
+        const CsrMatrix ref = g::spgemm(sa, sb);
+        REQUIRE(r1.rowPtr == ref.rowPtr && r1.columnIndices == ref.columnIndices && r1.values == ref.values);
+        REQUIRE(r2.values == r1.values && r1.rowPtr[1] == r1.rowPtr[2]);
+        caught = false;
+        try {
+            acc.addProduct(sb, sa);
+        } catch (const std::invalid_argument&) {
+            caught = true;
+        }
+        REQUIRE(caught);
+    }
+    {
+        g::LocalAccumulator<CsrMatrix> empty(0, 4);
+        REQUIRE(empty.finish().rowPtr == std::vector<int64_t>{0});
+    }
+    std::printf("shim_test: PASS\n");
+    return 0;
+}

@@ -195,6 +195,32 @@ def test_batch_equals_single(engine, port):
         assert csr_bits_equal(got, want), explain_diff(got, want)
 
 
+@pytest.mark.parametrize("mode", ["exact", "upper_bound"])
+def test_output_modes(port, mode):
+    import spgemm_gb300 as sg
+    with sg.Engine(0, mode=mode) as eng:
+        for seed in (1, 2):
+            a, b = row_sizes_for_bins(seed)
+            check(eng, port, a, b)
+        a = random_csr(300, 40, 25, 9, values="int")
+        b = random_csr(40, 50, 20, 10, values="int")
+        check(eng, port, a, b)  # many exact cancellations: rows shrink after summation
+        acc = eng.accumulate(40, 35, [(random_csr(40, 9, 5, 11), random_csr(9, 35, 6, 12, values="dyadic"))] * 3)
+        want = port.accumulate(40, 35, [(random_csr(40, 9, 5, 11), random_csr(9, 35, 6, 12, values="dyadic"))] * 3)
+        assert csr_bits_equal(acc, want), explain_diff(acc, want)
+
+
+def test_budget_exceeded(port):
+    import spgemm_gb300 as sg
+    a = random_csr(2000, 2000, 30, 13)
+    with sg.Engine(0, hbm_budget_bytes=64 << 10) as eng:
+        with pytest.raises(SpgError) as e:
+            eng.multiply(a, a)
+        assert e.value.name == "SPG_BUDGET_EXCEEDED"
+        small = random_csr(4, 4, 2, 14)
+        check(eng, port, small, small)
+
+
 def test_repeatable(engine):
     a = random_csr(500, 400, 30, 31)
     b = random_csr(400, 450, 25, 32)
