@@ -157,6 +157,29 @@ spg_status spg_accum_end(spg_handle* handle);
 spg_status spg_multiply_batch(spg_handle* handle, int32_t n, const spg_csr_view* A, const spg_csr_view* B,
                               int32_t out_location, spg_csr_result* C);
 
+/* ---- allocation-free product -------------------------------------------------
+ * No counterpart in the reference: its multiply always allocates its result.
+ * C = A * B for callers that cannot allocate memory when they multiply --
+ * code whose device memory is owned entirely by another allocator (a
+ * framework's caching pool or an arena reserved at start-up), real-time loops
+ * that forbid allocator calls after initialisation, host threads that must not
+ * take the allocator's locks.  A and B must be in device memory; the caller
+ * passes device arrays for C (row_ptr of A.rows+1 entries, col/val of
+ * c_capacity entries) and the stream to run on (NULL: the default stream); no
+ * handle is needed.  All scratch lives in one 32 MiB device array that the
+ * library reserves, once per GPU, for the life of the process; a product whose
+ * scratch would exceed it (roughly: 32 bytes per row of A plus 12 bytes per
+ * distinct output coordinate) is rejected with SPG_BUDGET_EXCEEDED, as is an
+ * nnz(C) above c_capacity (*c_nnz then holds the nnz needed).  The first call
+ * on a device looks up the array's device address, so make it before any
+ * stream capture.  Calls share the array: calls that overlap on the GPU race
+ * and must be serialised by the caller.  Results are those of spg_multiply.
+ * The call returns after the stream has finished the product; `err`
+ * (err_len bytes, may be NULL) receives a message on failure. */
+spg_status spg_multiply_noalloc(const spg_csr_view* A, const spg_csr_view* B, void* stream, int64_t* c_row_ptr,
+                                int32_t* c_col, double* c_val, int64_t c_capacity, int64_t* c_nnz, char* err,
+                                size_t err_len);
+
 /* ---- host staging helpers ------------------------------------------------- */
 /* Page-locked host memory (fast host<->device copies); free with spg_host_free. */
 void* spg_host_alloc(size_t bytes);
