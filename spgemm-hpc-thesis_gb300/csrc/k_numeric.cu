@@ -5,8 +5,9 @@
 //      its column, sequence number t and value __dmul_rn(a, b) (one rounding, as
 //      `const double product = aValue * b` in spgemm_exchange.cpp:287);
 //   2. sorts the products by column with a stable LSD radix sort (8-bit digits
-//      over the bits of max(col) - min(col) only; ranks from __match_any_sync
-//      and per-warp digit counters), so that equal columns stay in product order.
+//      over the bits of max(col) - min(col) only; ranks from ballot-matched
+//      lane groups and per-warp digit counters), so that equal columns stay in
+//      product order.
 //      When the column range and the sequence number fit in 32 bits together,
 //      the sort moves one packed word (column - min) << s | seq per product;
 //      otherwise it moves the column and a 16-bit sequence number side by side;
@@ -80,13 +81,26 @@ __device__ inline void scan_counters(uint32_t* c, int64_t* tmp) {
     }
 }
 
+// Lanes of the warp holding the same 8-bit digit: the intersection of one
+// ballot per digit bit (a ballot for each set bit, its complement for each
+// clear bit).  Eight votes cost a fraction of one __match_any_sync on GB300.
+__device__ inline unsigned digit_peers(uint32_t d) {
+    unsigned peers = 0xffffffffu;
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+        const unsigned set = __ballot_sync(0xffffffffu, (d >> b) & 1u);
+        peers &= ((d >> b) & 1u) ? set : ~set;
+    }
+    return peers;
+}
+
 // Stable rank of one striped item against this warp's digit counters: the
-// group of lanes holding the same digit is found with __match_any_sync; its
-// first lane advances the counter by the group size (one shared atomic) and
-// broadcasts the old value.  Items of a warp are ranked in order, so ranks
-// follow (warp, item, lane) order.
+// group of lanes holding the same digit (digit_peers); its first lane advances
+// the counter by the group size (one shared atomic) and broadcasts the old
+// value.  Items of a warp are ranked in order, so ranks follow
+// (warp, item, lane) order.
 __device__ inline uint32_t rank_item(uint32_t d, uint32_t* counter_of_d, int lane) {
-    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const unsigned peers = digit_peers(d);
     const int leader = __ffs(peers) - 1;
     uint32_t base = 0;
     if (lane == leader) base = atomicAdd(counter_of_d, static_cast<uint32_t>(__popc(peers)));
