@@ -325,6 +325,7 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
     for (int j = 0; j < njobs; ++j) {
         jobs[j].c_col = c_col;
         jobs[j].c_val = c_val;
+        jobs[j].holes = exact ? 0 : 1;
     }
     check_cuda(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(Job) * njobs, cudaMemcpyHostToDevice, st), "H2D jobs");
     for (int b = 1; b < kNumBins; ++b)
@@ -345,11 +346,14 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
     double* final_val = c_val;
     if (nz_total != tmp_total) {  // rows with fewer entries than reserved: compact
         launch_scan(nz, static_cast<int64_t>(slots) - 1, partials, st);
-        launches += 3 + njobs;
+        launches += 3 + (exact ? njobs : 1);
         final_col = ar.alloc<int32_t>(static_cast<size_t>(nz_total), "C col (compact)");
         final_val = ar.alloc<double>(static_cast<size_t>(nz_total), "C val (compact)");
-        for (int j = 0; j < njobs; ++j)
-            launch_compact(d_jobs + j, in[j].A->rows, final_col, final_val, st);
+        if (exact) {
+            for (int j = 0; j < njobs; ++j) launch_compact(d_jobs + j, in[j].A->rows, final_col, final_val, st);
+        } else {
+            launch_compact_holes(d_jobs, njobs, d_row_base, total_rows, final_col, final_val, st);
+        }
         check_cuda(cudaGetLastError(), "K5 launch");
         final_rp = nz;
         ar.free_now(c_col);

@@ -38,13 +38,14 @@ struct RowSmem {
     static constexpr int kCap = W * 32 * ITEMS;
     static constexpr int kSeqBits = log2_ceil_c(kCap);
     double vals[kCap];          // product values by sequence number; run sums in place
-    SegTab<W * 32> seg;         // enumeration batch
+    SegTab<W * 32, int32_t> seg;  // enumeration batch
     int64_t warp_tmp[W + 1];    // block scans
     uint32_t keys[kCap];        // columns (unpacked) or packed (column, sequence) words
     uint32_t hist[256 * W];     // digit counters, digit-major
     uint32_t cnt[W * ITEMS];    // kept entries per (warp, item)
     uint16_t seqs[kCap];        // sequence numbers of the unpacked path
     int32_t red[2 * W];         // min / max column reduction
+    uint32_t kept;              // stored entries of the row (upper-bound mode)
 };
 
 // Exclusive scan of the 256*W digit counters, 8 consecutive counters per thread.
@@ -88,8 +89,9 @@ __device__ inline unsigned digit_peers(uint32_t d) {
     unsigned peers = 0xffffffffu;
 #pragma unroll
     for (int b = 0; b < 8; ++b) {
-        const unsigned set = __ballot_sync(0xffffffffu, (d >> b) & 1u);
-        peers &= ((d >> b) & 1u) ? set : ~set;
+        const unsigned bit = (d >> b) & 1u;
+        const unsigned set = __ballot_sync(0xffffffffu, bit);
+        peers &= set ^ (bit - 1u);  // set where this lane's bit is 1, ~set where it is 0
     }
     return peers;
 }
@@ -135,52 +137,25 @@ __device__ inline void scan_kept(uint32_t* cnt, int32_t* red, int warp, int lane
     }
 }
 
-template <int W, int ITEMS>
-__device__ void numeric_row(const Job& J, int row, RowSmem<W, ITEMS>& sm, ErrWord* err) {
+// Where a row's result goes, read once from the Job (locals, not reloaded
+// through the Job reference after every global store).
+struct RowOut {
+    int32_t* __restrict__ c_col;
+    double* __restrict__ c_val;
+    int64_t out0;       // first slot of the row in C_tmp
+    int64_t* nz;        // the row's stored-entry count
+    int32_t holes;      // upper-bound mode: slot-per-position output with holes
+};
+
+// Steps 2-4 of a row for one key layout (PACKED: (col - cmin) << kSeqBits | seq
+// words; otherwise columns and 16-bit sequence numbers).
+template <int W, int ITEMS, bool PACKED>
+__device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS>& sm, int P, uint32_t cmin, int nbits, int lane,
+                           int warp, int tid) {
     using Sm = RowSmem<W, ITEMS>;
     constexpr int kSeqBits = Sm::kSeqBits;
-    const int lane = threadIdx.x & 31;
-    const int warp = W == 1 ? 0 : (threadIdx.x >> 5);
-    const int tid = W == 1 ? lane : threadIdx.x;
-    const int P = static_cast<int>(J.ub[row]);
-
-    // 1. products into shared memory
-    int32_t lo = INT32_MAX, hi = INT32_MIN;
-    const int32_t ncols = J.B.cols;
-    team_products<W * 32, true>(J, row, sm.seg, sm.warp_tmp, tid, [&](int64_t seq, int32_t c, double b, double a) {
-        if (c < 0 || c >= ncols) {
-            raise_error(err, kErrInvalid, 4, c);
-            c = 0;
-        }
-        sm.keys[seq] = static_cast<uint32_t>(c);
-        sm.vals[seq] = __dmul_rn(a, b);
-        lo = min(lo, c);
-        hi = max(hi, c);
-    });
-    lo = warp_min(lo);
-    hi = warp_max(hi);
-    if (W > 1) {
-        if (lane == 0) {
-            sm.red[warp] = lo;
-            sm.red[W + warp] = hi;
-        }
-        __syncthreads();
-        lo = sm.red[0];
-        hi = sm.red[W];
-#pragma unroll
-        for (int w = 1; w < W; ++w) {
-            lo = min(lo, sm.red[w]);
-            hi = max(hi, sm.red[W + w]);
-        }
-    }
-    row_sync<W>();
-    const uint32_t cmin = static_cast<uint32_t>(lo);
-    const uint32_t range = P ? static_cast<uint32_t>(hi - lo) : 0u;
-    const int nbits = range ? 32 - __clz(range) : 0;
-    const bool packed = nbits + kSeqBits <= 32;
-
     // 2. stable LSD radix sort by column
-    if (packed) {
+    if constexpr (PACKED) {
         // Packed words (col - cmin) << kSeqBits | seq; the first pass packs.
         for (int shift = 0; shift < nbits || shift == 0; shift += 8) {
             uint32_t k[ITEMS], rk[ITEMS];
@@ -259,11 +234,48 @@ __device__ void numeric_row(const Job& J, int row, RowSmem<W, ITEMS>& sm, ErrWor
 
     // Column and sequence number of sorted position pos.
     auto col_at = [&](int pos) -> uint32_t {
-        return packed ? (sm.keys[pos] >> kSeqBits) : sm.keys[pos] - cmin;
+        return PACKED ? (sm.keys[pos] >> kSeqBits) : sm.keys[pos] - cmin;
     };
     auto seq_at = [&](int pos) -> uint32_t {
-        return packed ? (sm.keys[pos] & ((1u << kSeqBits) - 1u)) : sm.seqs[pos];
+        return PACKED ? (sm.keys[pos] & ((1u << kSeqBits) - 1u)) : sm.seqs[pos];
     };
+
+    if (out.holes) {
+        // 3+4 in one pass (upper-bound mode): sorted position pos owns slot
+        // out0 + pos of the row's reserved range; the first position of every run
+        // writes (column, sum) when the sum is != 0, every other slot column -1.
+        const int64_t out0 = out.out0;
+        uint32_t kept = 0;
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i) {
+            const int pos = (warp * ITEMS + i) * 32 + lane;
+            if (pos < P) {
+                const uint32_t c = col_at(pos);
+                int32_t oc = -1;
+                double acc = 0.0;
+                if (pos == 0 || col_at(pos - 1) != c) {
+                    acc = sm.vals[seq_at(pos)];
+                    for (int q = pos + 1; q < P && col_at(q) == c; ++q) acc = __dadd_rn(acc, sm.vals[seq_at(q)]);
+                    if (acc != 0.0) {
+                        oc = static_cast<int32_t>(c + cmin);
+                        ++kept;
+                    }
+                }
+                out.c_col[out0 + pos] = oc;
+                if (oc >= 0) out.c_val[out0 + pos] = acc;
+            }
+        }
+        kept = warp_sum(kept);
+        if (W == 1) {
+            if (lane == 0) *out.nz = kept;
+        } else {
+            if (lane == 0) atomicAdd(&sm.kept, kept);
+            __syncthreads();
+            if (tid == 0) *out.nz = sm.kept;
+        }
+        row_sync<W>();
+        return;
+    }
 
     // 3. runs of equal columns summed in product order; each run's sum is stored
     //    in place of its first product's value
@@ -289,7 +301,7 @@ __device__ void numeric_row(const Job& J, int row, RowSmem<W, ITEMS>& sm, ErrWor
     row_sync<W>();
 
     // 4. kept (column, sum) pairs in sorted order
-    const int64_t out0 = J.cnt[row];
+    const int64_t out0 = out.out0;
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i) {
         const int pos = (warp * ITEMS + i) * 32 + lane;
@@ -306,12 +318,61 @@ __device__ void numeric_row(const Job& J, int row, RowSmem<W, ITEMS>& sm, ErrWor
         const unsigned m = __ballot_sync(0xffffffffu, keep);
         if (keep) {
             const int64_t idx = out0 + sm.cnt[warp * ITEMS + i] + __popc(m & lanemask_lt());
-            J.c_col[idx] = static_cast<int32_t>(c + cmin);
-            J.c_val[idx] = v;
+            out.c_col[idx] = static_cast<int32_t>(c + cmin);
+            out.c_val[idx] = v;
         }
     }
-    if (tid == 0) J.nz[row] = sm.red[0];
+    if (tid == 0) *out.nz = sm.red[0];
     row_sync<W>();
+}
+
+
+template <int W, int ITEMS>
+__device__ void numeric_row(const Job& J, int row, RowSmem<W, ITEMS>& sm, ErrWord* err) {
+    using Sm = RowSmem<W, ITEMS>;
+    constexpr int kSeqBits = Sm::kSeqBits;
+    const int lane = threadIdx.x & 31;
+    const int warp = W == 1 ? 0 : (threadIdx.x >> 5);
+    const int tid = W == 1 ? lane : threadIdx.x;
+    const int P = static_cast<int>(J.ub[row]);
+    if (W > 1 && tid == 0) sm.kept = 0;  // read only after the barriers below
+
+    // 1. products into shared memory
+    int32_t lo = INT32_MAX, hi = INT32_MIN;
+    const int32_t ncols = J.B.cols;
+    team_products<W * 32, true, int32_t>(J, row, sm.seg, sm.warp_tmp, tid, [&](int32_t seq, int32_t c, double b, double a) {
+        if (c < 0 || c >= ncols) {
+            raise_error(err, kErrInvalid, 4, c);
+            c = 0;
+        }
+        sm.keys[seq] = static_cast<uint32_t>(c);
+        sm.vals[seq] = __dmul_rn(a, b);
+        lo = min(lo, c);
+        hi = max(hi, c);
+    });
+    lo = warp_min(lo);
+    hi = warp_max(hi);
+    if (W > 1) {
+        if (lane == 0) {
+            sm.red[warp] = lo;
+            sm.red[W + warp] = hi;
+        }
+        __syncthreads();
+        lo = sm.red[0];
+        hi = sm.red[W];
+#pragma unroll
+        for (int w = 1; w < W; ++w) {
+            lo = min(lo, sm.red[w]);
+            hi = max(hi, sm.red[W + w]);
+        }
+    }
+    row_sync<W>();
+    const uint32_t cmin = static_cast<uint32_t>(lo);
+    const uint32_t range = P ? static_cast<uint32_t>(hi - lo) : 0u;
+    const int nbits = range ? 32 - __clz(range) : 0;
+    const RowOut out{J.c_col, J.c_val, J.cnt[row], J.nz + row, J.holes};
+    if (nbits + kSeqBits <= 32) finish_row<W, ITEMS, true>(out, sm, P, cmin, nbits, lane, warp, tid);
+    else finish_row<W, ITEMS, false>(out, sm, P, cmin, nbits, lane, warp, tid);
 }
 
 constexpr int kWarpKernelThreads = 256;
@@ -557,6 +618,8 @@ num_heavy_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items
             if (tid == 0) sm.out_base += static_cast<uint32_t>(sm.red[0]);
             __syncthreads();
         }
+        if (J.holes)  // upper-bound mode: the unused tail of the reserved range becomes holes
+            for (int64_t q = out0 + sm.out_base + tid; q < out0 + P; q += kHeavyThreads) J.c_col[q] = -1;
         if (tid == 0) {
             J.nz[row] = sm.out_base;
             kept_total += sm.out_base;

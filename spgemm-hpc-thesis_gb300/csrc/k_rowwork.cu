@@ -219,6 +219,46 @@ compact_kernel(const Job* __restrict__ job, int rows, int32_t* __restrict__ out_
     }
 }
 
+// K5 for rows written with holes (upper-bound mode): warp per row, the row's
+// reserved slots [cnt[r], cnt[r+1]) are read in order and the slots with a
+// column >= 0 are packed at the row's final offset nz[r] (ballot + popc).
+__global__ void __launch_bounds__(256)
+compact_holes_kernel(const Job* __restrict__ jobs, int njobs, const int64_t* __restrict__ job_row_base,
+                     int64_t total_rows, int32_t* __restrict__ out_col, double* __restrict__ out_val) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
+    for (int64_t g = static_cast<int64_t>(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5); g < total_rows;
+         g += warps) {
+        const int j = job_of_row(job_row_base, njobs, g);
+        const Job& J = jobs[j];
+        const int r = static_cast<int>(g - job_row_base[j]);
+        const int64_t src = J.cnt[r], end = J.cnt[r + 1];
+        int64_t dst = J.nz[r];
+        // four chunks of 32 slots per step; columns and values are loaded together
+        // (a hole's value is read and dropped) so the loads do not wait on each other
+        for (int64_t q0 = src; q0 < end; q0 += 128) {
+            int32_t c[4];
+            double v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int64_t q = q0 + u * 32 + lane;
+                c[u] = q < end ? J.c_col[q] : -1;
+                v[u] = q < end ? J.c_val[q] : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const unsigned m = __ballot_sync(0xffffffffu, c[u] >= 0);
+                if (c[u] >= 0) {
+                    const int64_t at = dst + __popc(m & lanemask_lt());
+                    out_col[at] = c[u];
+                    out_val[at] = v[u];
+                }
+                dst += __popc(m);
+            }
+        }
+    }
+}
+
 __global__ void gather_kernel(const int64_t* __restrict__ src, const int64_t* __restrict__ idx,
                               int64_t* __restrict__ dst, int n) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[idx[i]];
@@ -277,6 +317,13 @@ void launch_scan(int64_t* d_data, int64_t n, int64_t* d_partials, cudaStream_t s
 void launch_compact(const Job* d_job, int rows, int32_t* out_col, double* out_val, cudaStream_t stream) {
     if (rows <= 0) return;
     compact_kernel<<<grid_for(rows, 8, 152 * 16), 256, 0, stream>>>(d_job, rows, out_col, out_val);
+}
+
+void launch_compact_holes(const Job* d_jobs, int njobs, const int64_t* d_job_row_base, int64_t total_rows,
+                          int32_t* out_col, double* out_val, cudaStream_t stream) {
+    if (total_rows <= 0) return;
+    compact_holes_kernel<<<grid_for(total_rows, 8, 152 * 32), 256, 0, stream>>>(d_jobs, njobs, d_job_row_base,
+                                                                              total_rows, out_col, out_val);
 }
 
 void launch_gather(const int64_t* d_src, const int64_t* d_idx, int64_t* d_dst, int n, cudaStream_t stream) {

@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(kSymWarpThreads)
 sym_warp_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items, int64_t count, int tiny,
                 ErrWord* __restrict__ err) {
     __shared__ int32_t s_tab[kSymWarpThreads / 32][kSymWarpTable];
-    __shared__ SegTab<32> s_seg[kSymWarpThreads / 32];
+    __shared__ SegTab<32, int32_t> s_seg[kSymWarpThreads / 32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t warps = static_cast<int64_t>(gridDim.x) * (kSymWarpThreads / 32);
     for (int64_t i = static_cast<int64_t>(blockIdx.x) * (kSymWarpThreads / 32) + w; i < count; i += warps) {
@@ -56,7 +56,7 @@ sym_warp_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items,
         if (tiny) {
             // <= 32 products: product t goes to lane t; count the first lane of each column group.
             int32_t* stage = s_tab[w];
-            team_products<32, false>(J, row, s_seg[w], nullptr, lane, [&](int64_t seq, int32_t c, double, double) {
+            team_products<32, false, int32_t>(J, row, s_seg[w], nullptr, lane, [&](int32_t seq, int32_t c, double, double) {
                 stage[seq] = c;
             });
             __syncwarp();
@@ -74,7 +74,7 @@ sym_warp_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items,
             for (uint32_t s = lane; s < tsize; s += 32) tab[s] = -1;
             __syncwarp();
             int mine = 0;
-            team_products<32, false>(J, row, s_seg[w], nullptr, lane, [&](int64_t, int32_t c, double, double) {
+            team_products<32, false, int32_t>(J, row, s_seg[w], nullptr, lane, [&](int32_t, int32_t c, double, double) {
                 if (col_ok(c, J.B.cols, err)) mine += hash_insert(tab, mask, log2t, c);
             });
             found = warp_sum(mine);
@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(kSymBlockThreads)
 sym_block_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items, int64_t count,
                  ErrWord* __restrict__ err) {
     extern __shared__ int32_t s_tab[];  // kSymBlockTable slots
-    __shared__ SegTab<kSymBlockThreads> s_seg;
+    __shared__ SegTab<kSymBlockThreads, int32_t> s_seg;
     __shared__ int64_t s_warp[kSymBlockThreads / 32 + 1];
     __shared__ int s_found;
     for (int64_t i = blockIdx.x; i < count; i += gridDim.x) {
@@ -101,8 +101,8 @@ sym_block_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items
         if (threadIdx.x == 0) s_found = 0;
         __syncthreads();
         int mine = 0;
-        team_products<kSymBlockThreads, false>(J, row, s_seg, s_warp, threadIdx.x,
-                                               [&](int64_t, int32_t c, double, double) {
+        team_products<kSymBlockThreads, false, int32_t>(J, row, s_seg, s_warp, threadIdx.x,
+                                                        [&](int32_t, int32_t c, double, double) {
             if (col_ok(c, J.B.cols, err)) mine += hash_insert(s_tab, mask, log2t, c);
         });
         mine = warp_sum(mine);

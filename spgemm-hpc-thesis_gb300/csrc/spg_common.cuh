@@ -37,6 +37,8 @@ struct Job {
     int32_t* c_col = nullptr; // C_tmp columns (size = total of cnt)
     double* c_val = nullptr;  // C_tmp values
     int64_t row_base = 0;     // first flattened row of this job in a batch
+    int32_t holes = 0;        // 1: rows are written slot by slot into their reserved C_tmp range,
+                              // column -1 marking unused slots (upper-bound mode); 0: compacted
 };
 
 // Row bins by product count (ub).  Bin b covers (kBinHi[b-1], kBinHi[b]].
@@ -185,6 +187,9 @@ void launch_numeric(int bin, const Job* d_jobs, const int64_t* d_items, int64_t 
 size_t numeric_scratch_bytes(int bin, int64_t max_ub, int64_t count, int num_sms);
 // K5: move rows from C_tmp (offsets job.cnt) to C (offsets job.nz, scanned).
 void launch_compact(const Job* d_job, int rows, int32_t* out_col, double* out_val, cudaStream_t stream);
+// K5 for rows written with holes: keeps the slots whose column is >= 0.
+void launch_compact_holes(const Job* d_jobs, int njobs, const int64_t* d_job_row_base, int64_t total_rows,
+                          int32_t* out_col, double* out_val, cudaStream_t stream);
 // Bin list offsets from the bin histogram.
 void launch_bin_offsets(const Stats* d_stats, int64_t* d_bin_off, cudaStream_t stream);
 

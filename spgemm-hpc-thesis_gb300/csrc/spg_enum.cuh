@@ -20,23 +20,26 @@
 
 namespace spg {
 
-template <int N>
+// Idx is int32_t for rows of at most 2^31 - 1 products (every shared-memory
+// path), int64_t otherwise.
+template <int N, typename Idx = int64_t>
 struct SegTab {
     const int32_t* colp[N];
     const double* valp[N];
     double scale[N];
-    int64_t incl[N];  // inclusive prefix of segment lengths within the batch
+    Idx incl[N];  // inclusive prefix of segment lengths within the batch
 };
 
 // Segment e of a row (e counts the addend first when present).
+template <typename Idx>
 __device__ inline void row_segment(const Job& J, int row, int64_t a0, bool has_s, int64_t e,
-                                   const int32_t*& cp, const double*& vp, double& sc, int64_t& len) {
+                                   const int32_t*& cp, const double*& vp, double& sc, Idx& len) {
     if (has_s && e == 0) {
         const int64_t s0 = J.S.rp[row];
         cp = J.S.ci + s0;
         vp = J.S.v + s0;
         sc = 1.0;
-        len = J.S.rp[row + 1] - s0;
+        len = static_cast<Idx>(J.S.rp[row + 1] - s0);
     } else {
         const int64_t p = a0 + e - (has_s ? 1 : 0);
         const int32_t k = J.A.ci[p];
@@ -44,13 +47,13 @@ __device__ inline void row_segment(const Job& J, int row, int64_t a0, bool has_s
         cp = J.B.ci + b0;
         vp = J.B.v + b0;
         sc = J.A.v[p];
-        len = J.B.rp[k + 1] - b0;
+        len = static_cast<Idx>(J.B.rp[k + 1] - b0);
     }
 }
 
 // Smallest j in [0, N) with incl[j] > t (the batch total exceeds t).
-template <int N>
-__device__ inline int seg_search(const int64_t* incl, int64_t t) {
+template <int N, typename Idx>
+__device__ inline int seg_search(const Idx* incl, Idx t) {
     int j = 0;
 #pragma unroll
     for (int step = N / 2; step >= 1; step >>= 1)
@@ -58,21 +61,21 @@ __device__ inline int seg_search(const int64_t* incl, int64_t t) {
     return j;
 }
 
-// Inclusive block scan of int64 (NT threads, NT/32 <= 32 warps).
-template <int NT>
-__device__ inline int64_t block_incl_scan(int64_t v, int64_t* s_warp /* NT/32 + 1 */) {
+// Inclusive block scan (NT threads, NT/32 <= 32 warps).
+template <int NT, typename Idx>
+__device__ inline Idx block_incl_scan(Idx v, int64_t* s_warp /* NT/32 + 1 */) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     constexpr int NW = NT / 32;
-    const int64_t incl = warp_incl_scan(v, lane);
+    const Idx incl = warp_incl_scan(v, lane);
     if (lane == 31) s_warp[warp] = incl;
     __syncthreads();
     if (warp == 0) {
-        const int64_t w = lane < NW ? s_warp[lane] : 0;
-        const int64_t wi = warp_incl_scan(w, lane);
+        const Idx w = lane < NW ? static_cast<Idx>(s_warp[lane]) : Idx{0};
+        const Idx wi = warp_incl_scan(w, lane);
         if (lane < NW) s_warp[lane] = wi - w;
     }
     __syncthreads();
-    const int64_t out = incl + s_warp[warp];
+    const Idx out = incl + static_cast<Idx>(s_warp[warp]);
     __syncthreads();
     return out;
 }
@@ -87,21 +90,24 @@ __device__ inline void team_sync() {
 // (NT == blockDim.x, tid = threadIdx.x); every thread of the team must call it.
 // f(seq, col, b, a) is called once per product by the thread that owns it, with
 // the B entry's column `col`, its value `b` and the scale `a` (the product is
-// a*b).  kLoadVal = false skips the value loads (b is then 0).
-template <int NT, bool kLoadVal, typename F>
-__device__ inline void team_products(const Job& J, int row, SegTab<NT>& tab, int64_t* s_warp, int tid, F&& f) {
+// a*b).  kLoadVal = false skips the value loads (b is then 0).  Idx is the
+// index type of sequence numbers within the row (int32_t when the row has fewer
+// than 2^31 products, which keeps the per-product search in 32-bit integers).
+template <int NT, bool kLoadVal, typename Idx = int64_t, typename F>
+__device__ inline void team_products(const Job& J, int row, SegTab<NT, Idx>& tab, int64_t* s_warp, int tid,
+                                     F&& f) {
     const bool has_s = J.S.rp != nullptr;
     const int64_t a0 = J.A.rp[row];
     const int64_t nseg = (J.A.rp[row + 1] - a0) + (has_s ? 1 : 0);
-    int64_t seq_base = 0;
+    Idx seq_base = 0;
     for (int64_t e0 = 0; e0 < nseg; e0 += NT) {
         const int64_t e = e0 + tid;
         const int32_t* cp = nullptr;
         const double* vp = nullptr;
         double sc = 1.0;
-        int64_t len = 0;
+        Idx len = 0;
         if (e < nseg) row_segment(J, row, a0, has_s, e, cp, vp, sc, len);
-        int64_t incl;
+        Idx incl;
         if constexpr (NT == 32) incl = warp_incl_scan(len, tid);
         else incl = block_incl_scan<NT>(len, s_warp);
         tab.colp[tid] = cp;
@@ -109,15 +115,15 @@ __device__ inline void team_products(const Job& J, int row, SegTab<NT>& tab, int
         tab.scale[tid] = sc;
         tab.incl[tid] = incl;
         team_sync<NT>();
-        const int64_t total = tab.incl[NT - 1];
-        for (int64_t t0 = tid; t0 < total; t0 += 4 * NT) {
+        const Idx total = tab.incl[NT - 1];
+        for (Idx t0 = tid; t0 < total; t0 += 4 * NT) {
             int j[4];
-            int64_t q[4];
+            Idx q[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
-                const int64_t t = t0 + u * NT;
+                const Idx t = t0 + u * NT;
                 j[u] = t < total ? seg_search<NT>(tab.incl, t) : 0;
-                q[u] = t < total ? t - (j[u] ? tab.incl[j[u] - 1] : 0) : 0;
+                q[u] = t < total ? t - (j[u] ? tab.incl[j[u] - 1] : Idx{0}) : Idx{0};
             }
             int32_t c[4];
             double b[4];
