@@ -85,7 +85,7 @@ typedef struct {
 typedef struct {
     float ms_rowwork, ms_symbolic, ms_scan, ms_numeric, ms_compact, ms_total;
     int64_t products, nnz, rows;
-    int64_t bin_rows[11];
+    int64_t bin_rows[12];  /* rows per product-count bin (see spg_timings users) */
     int64_t launches;  /* kernels this library launched for the call */
 } spg_timings;
 

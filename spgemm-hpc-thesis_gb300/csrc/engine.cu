@@ -287,10 +287,9 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
     // Output layout: in the upper-bound mode every row is written at the prefix
     // of its product count (ub) and compacted afterwards; in the exact mode a
     // symbolic phase counts the distinct columns of every row first.
-    const int64_t heavy = bin_count[kBinHeavy];
     const bool exact = use_exact_mode(h, products, ar.bytes());
-    size_t scratch_bytes = numeric_scratch_bytes(kBinHeavy, max_ub, heavy, h->num_sms);
-    if (exact) scratch_bytes = std::max(scratch_bytes, symbolic_scratch_bytes(kBinHeavy, max_ub, heavy, h->num_sms));
+    size_t scratch_bytes = numeric_scratch_bytes(bin_count, max_ub, h->num_sms);
+    if (exact) scratch_bytes = std::max(scratch_bytes, symbolic_scratch_bytes(bin_count, max_ub, h->num_sms));
     void* scratch = scratch_bytes ? ar.alloc<unsigned char>(scratch_bytes, "heavy scratch") : nullptr;
     int64_t* partials = ar.alloc<int64_t>(scan_partials_count(static_cast<int64_t>(slots)), "scan partials");
     for (int b = 1; b < kNumBins; ++b) launches += bin_count[b] > 0 ? (exact ? 2 : 1) : 0;

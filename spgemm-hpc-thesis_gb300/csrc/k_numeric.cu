@@ -19,7 +19,8 @@
 //      row's output offset (job.cnt[row]) and the kept count into job.nz[row].
 // Every coordinate is therefore bit-identical to the serial reference.  Rows of
 // <= 512 products run one per warp, rows of <= 8192 one per CTA with everything
-// in shared memory, heavier rows one per CTA with the sort in a global slab.
+// in shared memory, rows of <= 16384 one per CTA with the product values in a
+// global slab, heavier rows one per CTA with the sort in a global slab.
 #include "spg_enum.cuh"
 
 namespace spg {
@@ -33,11 +34,12 @@ __device__ inline void row_sync() {
 
 constexpr int log2_ceil_c(int x) { return x <= 1 ? 0 : 1 + log2_ceil_c((x + 1) / 2); }
 
-template <int W, int ITEMS>
+// SV: product values in shared memory (else in a per-CTA global slab).
+template <int W, int ITEMS, bool SV = true>
 struct RowSmem {
     static constexpr int kCap = W * 32 * ITEMS;
     static constexpr int kSeqBits = log2_ceil_c(kCap);
-    double vals[kCap];          // product values by sequence number; run sums in place
+    double vals[SV ? kCap : 1];  // product values by sequence number; run sums in place
     SegTab<W * 32, int32_t> seg;  // enumeration batch
     int64_t warp_tmp[W + 1];    // block scans
     uint32_t keys[kCap];        // columns (unpacked) or packed (column, sequence) words
@@ -149,10 +151,10 @@ struct RowOut {
 
 // Steps 2-4 of a row for one key layout (PACKED: (col - cmin) << kSeqBits | seq
 // words; otherwise columns and 16-bit sequence numbers).
-template <int W, int ITEMS, bool PACKED>
-__device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS>& sm, int P, uint32_t cmin, int nbits, int lane,
-                           int warp, int tid) {
-    using Sm = RowSmem<W, ITEMS>;
+template <int W, int ITEMS, bool SV, bool PACKED>
+__device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double* vals, int P, uint32_t cmin,
+                           int nbits, int lane, int warp, int tid) {
+    using Sm = RowSmem<W, ITEMS, SV>;
     constexpr int kSeqBits = Sm::kSeqBits;
     // 2. stable LSD radix sort by column
     if constexpr (PACKED) {
@@ -254,8 +256,8 @@ __device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS>& sm, int P, uint
                 int32_t oc = -1;
                 double acc = 0.0;
                 if (pos == 0 || col_at(pos - 1) != c) {
-                    acc = sm.vals[seq_at(pos)];
-                    for (int q = pos + 1; q < P && col_at(q) == c; ++q) acc = __dadd_rn(acc, sm.vals[seq_at(q)]);
+                    acc = vals[seq_at(pos)];
+                    for (int q = pos + 1; q < P && col_at(q) == c; ++q) acc = __dadd_rn(acc, vals[seq_at(q)]);
                     if (acc != 0.0) {
                         oc = static_cast<int32_t>(c + cmin);
                         ++kept;
@@ -287,9 +289,9 @@ __device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS>& sm, int P, uint
             const uint32_t c = col_at(pos);
             if (pos == 0 || col_at(pos - 1) != c) {
                 const uint32_t s0 = seq_at(pos);
-                double acc = sm.vals[s0];
-                for (int q = pos + 1; q < P && col_at(q) == c; ++q) acc = __dadd_rn(acc, sm.vals[seq_at(q)]);
-                sm.vals[s0] = acc;
+                double acc = vals[s0];
+                for (int q = pos + 1; q < P && col_at(q) == c; ++q) acc = __dadd_rn(acc, vals[seq_at(q)]);
+                vals[s0] = acc;
                 keep = acc != 0.0;
             }
         }
@@ -311,7 +313,7 @@ __device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS>& sm, int P, uint
         if (pos < P) {
             c = col_at(pos);
             if (pos == 0 || col_at(pos - 1) != c) {
-                v = sm.vals[seq_at(pos)];
+                v = vals[seq_at(pos)];
                 keep = v != 0.0;
             }
         }
@@ -327,9 +329,9 @@ __device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS>& sm, int P, uint
 }
 
 
-template <int W, int ITEMS>
-__device__ void numeric_row(const Job& J, int row, RowSmem<W, ITEMS>& sm, ErrWord* err) {
-    using Sm = RowSmem<W, ITEMS>;
+template <int W, int ITEMS, bool SV>
+__device__ void numeric_row(const Job& J, int row, RowSmem<W, ITEMS, SV>& sm, double* vals, ErrWord* err) {
+    using Sm = RowSmem<W, ITEMS, SV>;
     constexpr int kSeqBits = Sm::kSeqBits;
     const int lane = threadIdx.x & 31;
     const int warp = W == 1 ? 0 : (threadIdx.x >> 5);
@@ -346,7 +348,7 @@ __device__ void numeric_row(const Job& J, int row, RowSmem<W, ITEMS>& sm, ErrWor
             c = 0;
         }
         sm.keys[seq] = static_cast<uint32_t>(c);
-        sm.vals[seq] = __dmul_rn(a, b);
+        vals[seq] = __dmul_rn(a, b);
         lo = min(lo, c);
         hi = max(hi, c);
     });
@@ -371,8 +373,8 @@ __device__ void numeric_row(const Job& J, int row, RowSmem<W, ITEMS>& sm, ErrWor
     const uint32_t range = P ? static_cast<uint32_t>(hi - lo) : 0u;
     const int nbits = range ? 32 - __clz(range) : 0;
     const RowOut out{J.c_col, J.c_val, J.cnt[row], J.nz + row, J.holes};
-    if (nbits + kSeqBits <= 32) finish_row<W, ITEMS, true>(out, sm, P, cmin, nbits, lane, warp, tid);
-    else finish_row<W, ITEMS, false>(out, sm, P, cmin, nbits, lane, warp, tid);
+    if (nbits + kSeqBits <= 32) finish_row<W, ITEMS, SV, true>(out, sm, vals, P, cmin, nbits, lane, warp, tid);
+    else finish_row<W, ITEMS, SV, false>(out, sm, vals, P, cmin, nbits, lane, warp, tid);
 }
 
 constexpr int kWarpKernelThreads = 256;
@@ -394,7 +396,7 @@ num_warp_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items,
         const int64_t it = items[i];
         const Job& J = jobs[item_job(it)];
         const int row = item_row(it);
-        numeric_row<1, ITEMS>(J, row, sm, err);
+        numeric_row<1, ITEMS, true>(J, row, sm, sm.vals, err);
         if ((threadIdx.x & 31) == 0) mine += static_cast<unsigned long long>(J.nz[row]);
     }
     if ((threadIdx.x & 31) == 0 && mine) atomicAdd(&s_nz, mine);
@@ -402,19 +404,20 @@ num_warp_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items,
     if (threadIdx.x == 0 && s_nz) atomicAdd(&stats->nz_total, s_nz);
 }
 
-template <int W, int ITEMS, int MINB>
+template <int W, int ITEMS, int MINB, bool SV>
 __global__ void __launch_bounds__(W * 32, MINB)
 num_block_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items, int64_t count,
-                 Stats* __restrict__ stats, ErrWord* __restrict__ err) {
+                 Stats* __restrict__ stats, ErrWord* __restrict__ err, double* __restrict__ gvals) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    using Sm = RowSmem<W, ITEMS>;
+    using Sm = RowSmem<W, ITEMS, SV>;
     Sm& sm = *reinterpret_cast<Sm*>(smem_raw);
+    double* vals = SV ? sm.vals : gvals + static_cast<size_t>(blockIdx.x) * Sm::kCap;
     unsigned long long mine = 0;
     for (int64_t i = blockIdx.x; i < count; i += gridDim.x) {
         const int64_t it = items[i];
         const Job& J = jobs[item_job(it)];
         const int row = item_row(it);
-        numeric_row<W, ITEMS>(J, row, sm, err);
+        numeric_row<W, ITEMS, SV>(J, row, sm, vals, err);
         if (threadIdx.x == 0) mine += static_cast<unsigned long long>(J.nz[row]);
     }
     if (threadIdx.x == 0 && mine) atomicAdd(&stats->nz_total, mine);
@@ -635,6 +638,8 @@ int capped(int64_t work, int per_block, int cap) {
 }
 
 int heavy_grid(int64_t count, int num_sms) { return static_cast<int>(count < num_sms ? count : num_sms); }
+int slab_grid(int64_t count, int num_sms) { return static_cast<int>(count < num_sms ? count : num_sms); }
+constexpr int kB16Cap = 16 * 32 * 32;
 
 template <int ITEMS>
 void run_warp(const Job* jobs, const int64_t* items, int64_t count, Stats* stats, ErrWord* err, cudaStream_t st,
@@ -645,20 +650,24 @@ void run_warp(const Job* jobs, const int64_t* items, int64_t count, Stats* stats
                                                                                            err);
 }
 
-template <int W, int ITEMS, int MINB>
+template <int W, int ITEMS, int MINB, bool SV = true>
 void run_block(const Job* jobs, const int64_t* items, int64_t count, Stats* stats, ErrWord* err, cudaStream_t st,
-               int num_sms) {
-    const int smem = static_cast<int>(sizeof(RowSmem<W, ITEMS>));
-    cudaFuncSetAttribute(num_block_kernel<W, ITEMS, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    num_block_kernel<W, ITEMS, MINB><<<capped(count, 1, num_sms * 8), W * 32, smem, st>>>(jobs, items, count, stats,
-                                                                                         err);
+               int num_sms, double* gvals = nullptr) {
+    const int smem = static_cast<int>(sizeof(RowSmem<W, ITEMS, SV>));
+    cudaFuncSetAttribute(num_block_kernel<W, ITEMS, MINB, SV>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    const int grid = SV ? capped(count, 1, num_sms * 8) : slab_grid(count, num_sms);
+    num_block_kernel<W, ITEMS, MINB, SV><<<grid, W * 32, smem, st>>>(jobs, items, count, stats, err, gvals);
 }
 
 }  // namespace
 
-size_t numeric_scratch_bytes(int bin, int64_t max_ub, int64_t count, int num_sms) {
-    if (bin != kBinHeavy || count == 0) return 0;
-    return static_cast<size_t>(heavy_grid(count, num_sms)) * 24 * static_cast<size_t>(max_ub);
+size_t numeric_scratch_bytes(const int64_t* bin_count, int64_t max_ub, int num_sms) {
+    size_t b16 = 0, heavy = 0;
+    if (bin_count[kBinB16K])
+        b16 = static_cast<size_t>(slab_grid(bin_count[kBinB16K], num_sms)) * kB16Cap * sizeof(double);
+    if (bin_count[kBinHeavy])
+        heavy = static_cast<size_t>(heavy_grid(bin_count[kBinHeavy], num_sms)) * 24 * static_cast<size_t>(max_ub);
+    return b16 > heavy ? b16 : heavy;
 }
 
 void launch_numeric(int bin, const Job* d_jobs, const int64_t* d_items, int64_t count, int64_t max_ub,
@@ -674,6 +683,10 @@ void launch_numeric(int bin, const Job* d_jobs, const int64_t* d_items, int64_t 
         case kBinB2K: run_block<8, 8, 3>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;
         case kBinB4K: run_block<8, 16, 2>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;
         case kBinB8K: run_block<16, 16, 1>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;
+        case kBinB16K:
+            run_block<16, 32, 1, false>(d_jobs, d_items, count, d_stats, d_err, st, num_sms,
+                                        static_cast<double*>(d_scratch));
+            break;
         case kBinHeavy:
             num_heavy_kernel<<<heavy_grid(count, num_sms), kHeavyThreads, 0, st>>>(d_jobs, d_items, count, d_scratch,
                                                                                    max_ub, d_stats, d_err);

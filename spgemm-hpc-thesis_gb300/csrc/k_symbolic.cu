@@ -10,6 +10,8 @@
 //   * rows of <= 8192 products: one CTA per row, table in shared memory;
 //   * heavier rows: one CTA per row, table in a global-memory slab per CTA.
 // It also rejects B columns outside [0, B.cols).
+#include <algorithm>
+
 #include "spg_enum.cuh"
 
 namespace spg {
@@ -151,8 +153,9 @@ int heavy_ctas(int64_t count, int num_sms) { return static_cast<int>(count < num
 
 }  // namespace
 
-size_t symbolic_scratch_bytes(int bin, int64_t max_ub, int64_t count, int num_sms) {
-    if (bin != kBinHeavy || count == 0) return 0;
+size_t symbolic_scratch_bytes(const int64_t* bin_count, int64_t max_ub, int num_sms) {
+    const int64_t count = std::max(bin_count[kBinB16K], bin_count[kBinHeavy]);
+    if (count == 0) return 0;
     return static_cast<size_t>(heavy_ctas(count, num_sms)) * (size_t{1} << ceil_log2(2 * max_ub)) * sizeof(int32_t);
 }
 

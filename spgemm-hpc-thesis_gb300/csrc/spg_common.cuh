@@ -53,10 +53,11 @@ enum Bin : int {
     kBinB2K,   // <= 2048     8 warps x 8 items
     kBinB4K,   // <= 4096     8 warps x 16 items
     kBinB8K,   // <= 8192     16 warps x 16 items
-    kBinHeavy, // >  8192     one CTA per row, sort in global memory
+    kBinB16K,  // <= 16384    16 warps x 32 items, product values in a global slab
+    kBinHeavy, // >  16384    one CTA per row, sort in global memory
     kNumBins
 };
-constexpr int64_t kHeavyThreshold = 8192;
+constexpr int64_t kHeavyThreshold = 16384;
 
 __host__ __device__ inline int clz64(unsigned long long x) {
 #ifdef __CUDA_ARCH__
@@ -176,7 +177,8 @@ void launch_bin_scatter(const Job* d_jobs, int njobs, const int64_t* d_job_row_b
 void launch_symbolic(int bin, const Job* d_jobs, const int64_t* d_items, int64_t count, int64_t max_ub,
                      void* d_scratch, size_t scratch_bytes, Stats* d_stats, ErrWord* d_err,
                      cudaStream_t stream, int num_sms);
-size_t symbolic_scratch_bytes(int bin, int64_t max_ub, int64_t count, int num_sms);
+// Global scratch of the symbolic phase (hash slabs of rows above 8192 products).
+size_t symbolic_scratch_bytes(const int64_t* bin_count, int64_t max_ub, int num_sms);
 // K3: exclusive scan of n+1 int64 counts in place (last entry becomes the total).
 void launch_scan(int64_t* d_data, int64_t n, int64_t* d_partials, cudaStream_t stream);
 size_t scan_partials_count(int64_t n);
@@ -184,7 +186,9 @@ size_t scan_partials_count(int64_t n);
 void launch_numeric(int bin, const Job* d_jobs, const int64_t* d_items, int64_t count, int64_t max_ub,
                     void* d_scratch, size_t scratch_bytes, Stats* d_stats, ErrWord* d_err,
                     cudaStream_t stream, int num_sms);
-size_t numeric_scratch_bytes(int bin, int64_t max_ub, int64_t count, int num_sms);
+// Global scratch of the numeric phase (value slabs of the 16K bin, sort slabs
+// of heavy rows; the two launches run one after the other and share it).
+size_t numeric_scratch_bytes(const int64_t* bin_count, int64_t max_ub, int num_sms);
 // K5: move rows from C_tmp (offsets job.cnt) to C (offsets job.nz, scanned).
 void launch_compact(const Job* d_job, int rows, int32_t* out_col, double* out_val, cudaStream_t stream);
 // K5 for rows written with holes: keeps the slots whose column is >= 0.

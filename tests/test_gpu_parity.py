@@ -49,7 +49,8 @@ def test_every_bin(engine, port, seed):
     a, b = row_sizes_for_bins(seed)
     check(engine, port, a, b)
     t = engine.last_timings()
-    assert t["bin_rows"]["heavy"] >= 2 and t["bin_rows"]["b<=8K"] >= 1 and t["bin_rows"]["w<=32"] >= 1
+    assert t["bin_rows"]["heavy"] >= 2 and t["bin_rows"]["b<=16K"] >= 3 and t["bin_rows"]["b<=8K"] >= 1
+    assert t["bin_rows"]["w<=32"] >= 1
 
 
 def test_known_answer(engine):
