@@ -47,7 +47,13 @@ WORKLOADS = {
                 "70% within +-2048 band, FP64 U[-1,1)",
     "uniform": "C=A*B, A and B 65536^2, 16 distinct uniform columns per row, FP64 U[-1,1)",
     "galerkin": "R*A then (R*A)*R^T, A 7-point Laplacian on 128^3, R 2x2x2 aggregation (262144 x 2097152)",
+    "batched": "512 independent square C_i = A_i*B_i, rows log-uniform in [1000, 200000], 4-64 distinct uniform "
+               "columns per row, FP64 U[-1,1); admitted in waves under a 150 GB budget",
+    "served": "Poisson arrivals (50-2000 req/s) of products drawn from the uniform, power-law, Galerkin and "
+              "batched size distributions (<= 2M rows), device-resident operands, 150 GB admission budget",
 }
+BATCH_PRODUCTS = 512
+SERVE_RATES = (50, 100, 200, 500, 1000, 2000)
 
 
 def make_workload(name: str, rows: int = 0):
@@ -67,7 +73,37 @@ def make_workload(name: str, rows: int = 0):
         with sg.Engine(int(os.environ.get("LOCAL_RANK", "0"))) as eng:
             ra = eng.multiply(r, lap)
         return [(r, lap), (ra, rt)]
+    if name == "batched":
+        rng = np.random.default_rng(4)
+        sizes = np.exp(rng.uniform(np.log(1000), np.log(200000), size=BATCH_PRODUCTS)).astype(np.int64)
+        return [(sg.synth_uniform(int(n), int(n), 4, 64, seed=2 * i + 1),
+                 sg.synth_uniform(int(n), int(n), 4, 64, seed=2 * i + 2)) for i, n in enumerate(sizes)]
+    if name == "served":
+        return serve_pool()
     raise SystemExit(f"unknown workload {name}")
+
+
+def serve_pool():
+    """The request pool of the served stream: 6 products from each size
+    distribution (uniform 65536^2 x 16; power-law with 2^12-2^18 rows; Galerkin
+    R*A on 16^3-128^3 grids, 128^3 = 2,097,152 fine rows; the batched
+    distribution's 1000-200000 rows x 4-64)."""
+    import spgemm_gb300 as sg
+    rng = np.random.default_rng(5)
+    pool = []
+    for i in range(6):
+        pool.append((sg.synth_uniform(65536, 65536, 16, seed=100 + 2 * i),
+                     sg.synth_uniform(65536, 65536, 16, seed=101 + 2 * i)))
+    for i in range(6):
+        n = int(np.exp(rng.uniform(np.log(4096), np.log(262144))))
+        a = sg.synth_powerlaw(n, 24.0, 1.2, 20000, 2048, 0.7, seed=200 + i)
+        pool.append((a, a))
+    for g in (16, 32, 48, 64, 96, 128):
+        pool.append((sg.synth_restriction(g), sg.synth_laplacian3d(g)))
+    for i in range(6):
+        n = int(np.exp(rng.uniform(np.log(1000), np.log(200000))))
+        pool.append((sg.synth_uniform(n, n, 4, 64, seed=300 + 2 * i), sg.synth_uniform(n, n, 4, 64, seed=301 + 2 * i)))
+    return pool
 
 
 def peaks() -> dict:
@@ -388,6 +424,199 @@ def run_gpu_arm(args, rank, world, local):
     eng.close()
 
 
+def _wall(fn):
+    """Seconds of fn() between device synchronisations (work spread over the
+    server's streams has no single stream to put events on)."""
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = fn()
+    torch.cuda.synchronize()
+    return time.perf_counter() - t0, out
+
+
+def run_batched(args, rank, world, local):
+    """512 uneven products: all submitted to the serving loop at once (waves
+    formed by admission under the 150 GB budget, one launch per bin and phase
+    per wave) against the same products multiplied one call at a time."""
+    import torch
+    import spgemm_gb300 as sg
+    torch.cuda.set_device(local)
+    pairs = make_workload("batched")
+    products = [sg.scalar_products_host(a, b) for a, b in pairs]
+    total_p = sum(products)
+    dev = [(a.to_device(local), b.to_device(local)) for a, b in pairs]
+    in_bytes = sum(_csr_bytes(a) + _csr_bytes(b) for a, b in pairs)
+
+    def served(srv):
+        tickets = [srv.submit(a, b) for a, b in dev]
+        nnz, batches, launches = 0, {}, 0
+        for t in tickets:
+            st, res, info = srv.poll(t)
+            if st != "SPG_OK":
+                raise SystemExit(f"batched request failed: {st} {info}")
+            nnz += res.nnz
+            batches[info["batch_id"]] = (info["batch_requests"], info["batch_launches"])
+            res.free()
+        return nnz, batches
+
+    srv = sg.Server(local, lanes=2, max_batch=BATCH_PRODUCTS, hbm_budget_bytes=150 * 10**9)
+    for _ in range(args.warmup):
+        c_nnz, _ = served(srv)
+    times, waves, launches = [], [], 0
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            t, (_, batches) = _wall(lambda: served(srv))
+            times.append(t)
+            waves.append(sorted(n for n, _ in batches.values()))
+            launches += sum(l for _, l in batches.values())
+    srv.close()
+    t_batched = sum(times)
+    value = 2.0 * total_p * args.steps / t_batched / 1e9
+
+    eng = sg.Engine(local)
+
+    def one_by_one():
+        launches = 0
+        for a, b in dev:
+            r = eng.multiply(a, b, out="device")
+            launches += eng.last_timings()["launches"]
+            r.free()
+        return launches
+
+    one_by_one()
+    k1 = max(1, min(args.steps, 2))
+    t_single = 0.0
+    for _ in range(k1):
+        t, _ = _wall(one_by_one)
+        t_single += t
+    single = 2.0 * total_p * k1 / t_single / 1e9
+    eng.close()
+
+    c_bytes_alg = sum(sg.algorithmic_bytes(a, b, p, 0) for (a, b), p in zip(pairs, products)) + 12 * c_nnz
+    pk = peaks()
+    achieved = c_bytes_alg / (t_batched / args.steps) / 1e9
+    line = {
+        "metric": "GFLOP/s", "value": value, "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_batched / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOADS["batched"], "name": "batched", "products": len(pairs),
+                   "rows_total": int(sum(a.rows for a, _ in pairs)), "scalar_products_per_step": int(total_p),
+                   "c_nnz": int(c_nnz), "l2": f"inputs larger than L2 ({in_bytes / 1e9:.1f} GB, no flush)",
+                   "timing": "host wall clock between device synchronisations (two lanes, two streams)",
+                   "server": {"lanes": 2, "max_batch": BATCH_PRODUCTS, "hbm_budget_bytes": 150 * 10**9},
+                   "waves_per_step": [len(w) for w in waves], "wave_sizes_last_step": waves[-1]},
+        "per_product_launches": {"value": single, "unit": "GFLOP/s", "steps": k1,
+                                 "ms_per_step": 1e3 * t_single / k1,
+                                 "what": "the same 512 products, one spg_multiply call each"},
+        "batched_over_per_product": value / single,
+        "roofline": {"bound": "hbm", "kernel": "whole batched step", "achieved": achieved, "peak": pk["hbm_gbs"],
+                     "unit": "GB/s", "frac": achieved / pk["hbm_gbs"], "peak_source": pk["source"],
+                     "traffic": None, "bytes_alg": int(c_bytes_alg)},
+        "cpu_baseline": None, "e2e": None, "gpu_launches": int(launches), "clocks": clocks.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def _arrivals(rate: float, n: int, pool_size: int, seed: int):
+    rng = np.random.default_rng(seed)
+    return np.cumsum(rng.exponential(1.0 / rate, size=n)), rng.integers(0, pool_size, size=n)
+
+
+def _serve_trace(srv, dev, products, at, picks):
+    """Submits pool requests at the given arrival times (seconds) from one
+    thread while another collects them; returns per-request (latency ms) and
+    the span from first submit to last completion."""
+    n = len(at)
+    tickets = [None] * n
+    submit_t = [0.0] * n
+    ready = threading.Semaphore(0)
+
+    def submitter():
+        t0 = time.perf_counter()
+        for i in range(n):
+            d = t0 + at[i] - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            a, b = dev[picks[i]]
+            submit_t[i] = time.perf_counter()
+            tickets[i] = srv.submit(a, b)
+            ready.release()
+
+    th = threading.Thread(target=submitter)
+    th.start()
+    lat, done_t, batch_sizes, launches, seen = [], [], [], 0, set()
+    for i in range(n):
+        ready.acquire()
+        st, res, info = srv.poll(tickets[i])
+        if st != "SPG_OK":
+            raise SystemExit(f"served request failed: {st} {info}")
+        res.free()
+        lat.append(info["latency_ms"])
+        done_t.append(submit_t[i] + info["latency_ms"] / 1e3)
+        batch_sizes.append(info["batch_requests"])
+        if info["batch_id"] not in seen:
+            seen.add(info["batch_id"])
+            launches += info["batch_launches"]
+    th.join()
+    span = max(done_t) - min(submit_t)
+    p = sum(products[j] for j in picks)
+    lat = np.asarray(lat)
+    return {"requests": n, "req_per_s": n / span, "gflops": 2.0 * p / span / 1e9,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_batch": float(np.mean(batch_sizes)), "span_s": span, "launches": int(launches)}
+
+
+def run_served(args, rank, world, local):
+    """The served stream: one Poisson trace per rate, served by continuous
+    batching (3 lanes, batches of up to 256 requests / 2^29 scalar products)
+    and by per-request launches
+    (1 lane, batches of 1), plus both at saturation (every request queued at
+    once)."""
+    import torch
+    import spgemm_gb300 as sg
+    torch.cuda.set_device(local)
+    pool = make_workload("served")
+    products = [sg.scalar_products_host(a, b) for a, b in pool]
+    dev = [(a.to_device(local), b.to_device(local)) for a, b in pool]
+    modes = {"batched": dict(lanes=3, max_batch=256, max_batch_products=1 << 29),
+             "per_request": dict(lanes=1, max_batch=1)}
+    n_sat = 300
+    table = {m: {} for m in modes}
+    with ClockSampler(local) as clocks:
+        for mode, kw in modes.items():
+            with sg.Server(local, hbm_budget_bytes=150 * 10**9, **kw) as srv:
+                for w in range(args.warmup):  # every pool entry once per warm-up pass
+                    _serve_trace(srv, dev, products, np.zeros(len(pool)), np.arange(len(pool)))
+                at, picks = _arrivals(1.0, n_sat, len(pool), seed=7)
+                table[mode]["saturation"] = _serve_trace(srv, dev, products, np.zeros(n_sat), picks)
+                for rate in SERVE_RATES:
+                    n = int(min(400, max(100, 3 * rate)))
+                    at, picks = _arrivals(rate, n, len(pool), seed=rate)
+                    table[mode][str(rate)] = _serve_trace(srv, dev, products, at, picks)
+    sat_b, sat_p = table["batched"]["saturation"], table["per_request"]["saturation"]
+    line = {
+        "metric": "served products/s", "value": sat_b["req_per_s"], "unit": "products/s", "n_gpus": world,
+        "steps": 1, "warmup": args.warmup, "ms_per_step": 1e3 * sat_b["span_s"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOADS["served"], "name": "served", "pool": len(pool),
+                   "pool_products": [int(p) for p in products], "rates_req_per_s": list(SERVE_RATES),
+                   "saturation_requests": n_sat, "timing": "server-side submit-to-ready latency; span on the host clock",
+                   "modes": modes, "hbm_budget_bytes": 150 * 10**9},
+        "gflops_saturation": sat_b["gflops"],
+        "per_request_launches": {"value": sat_p["req_per_s"], "unit": "products/s", "gflops": sat_p["gflops"],
+                                 "p50_ms": sat_p["p50_ms"], "p99_ms": sat_p["p99_ms"]},
+        "batched_over_per_request": sat_b["req_per_s"] / sat_p["req_per_s"],
+        "p50_ms": sat_b["p50_ms"], "p99_ms": sat_b["p99_ms"],
+        "by_rate": table, "roofline": None, "cpu_baseline": None, "e2e": None,
+        "gpu_launches": int(sum(v["launches"] for m in table.values() for v in m.values())),
+        "clocks": clocks.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line))
+
+
 def _pinned_like(n, dtype):
     import torch
     return torch.empty(max(int(n), 1), dtype=dtype, pin_memory=True)
@@ -427,6 +656,10 @@ def main():
     rank, world, local = dist_init()
     if args.impl == "reference":
         run_reference_arm(args, rank, world)
+    elif args.workload == "batched":
+        run_batched(args, rank, world, local)
+    elif args.workload == "served":
+        run_served(args, rank, world, local)
     else:
         run_gpu_arm(args, rank, world, local)
 

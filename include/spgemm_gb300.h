@@ -157,6 +157,72 @@ spg_status spg_accum_end(spg_handle* handle);
 spg_status spg_multiply_batch(spg_handle* handle, int32_t n, const spg_csr_view* A, const spg_csr_view* B,
                               int32_t out_location, spg_csr_result* C);
 
+/* Scalar products of every product of a batch (one counting pass for all):
+ * products[i] = P of A[i] * B[i]; errors as spg_scalar_multiplication_count. */
+spg_status spg_scalar_multiplication_count_batch(spg_handle* handle, int32_t n, const spg_csr_view* A,
+                                                 const spg_csr_view* B, int64_t* products);
+
+/* ---- serving loop ---------------------------------------------------------------
+ * No reference counterpart (the reference runs one product per call).  A
+ * server accepts products as they arrive and runs them in batches on one GPU:
+ * `lanes` worker threads, each with its own stream, take the longest prefix
+ * of the FIFO queue whose footprint fits the free part of the HBM budget (at
+ * most max_batch requests and about max_batch_products scalar products) and
+ * multiply it as one spg_multiply_batch; while
+ * one batch runs, the next lane admits what arrived meanwhile, so batches
+ * overlap on the device.  A request's footprint is its upper-bound device
+ * memory: 36 bytes per scalar product + 40 bytes per row of A + its staged
+ * host operands + 4 MiB; an uncollected device result stays charged (its own
+ * size) until spg_poll returns it.  A request that can never fit fails with
+ * SPG_BUDGET_EXCEEDED; an input error fails only the request that has it.
+ * Results are bit-identical to spg_multiply of the same operands, alone or in
+ * any mix.  Operand arrays must stay valid until the request's spg_poll has
+ * returned something other than SPG_NOT_READY. */
+typedef struct spg_server spg_server;
+
+typedef struct {
+    int32_t device;
+    int32_t lanes;              /* batches in flight at once (worker threads/streams); default 2 */
+    int32_t max_batch;          /* most requests per batch; 1 runs every request alone; default 256 */
+    int32_t out_location;       /* where results are delivered (spg_location); default SPG_DEVICE */
+    int32_t mode;               /* spg_mode of the products; default SPG_MODE_AUTO */
+    int32_t reserved;
+    uint64_t hbm_budget_bytes;  /* admission budget for in-flight work; default 150 GB */
+    int64_t max_batch_products; /* a batch stops growing past this many scalar products (a lone larger
+                                   request still runs), so that a long queue splits over the lanes;
+                                   default 2^30 */
+} spg_server_config;
+
+typedef struct {
+    double queue_ms;            /* submit -> admitted to a batch */
+    double service_ms;          /* admitted -> result ready */
+    double latency_ms;          /* submit -> result ready */
+    int64_t products;           /* scalar products of the request */
+    int64_t footprint_bytes;    /* admission charge */
+    int32_t batch_requests;     /* requests in the batch that served it */
+    int32_t lane;               /* worker lane that served it (-1: never ran) */
+    uint64_t batch_id;          /* the batch that served it (0: never ran) */
+    int64_t batch_launches;     /* kernels that batch launched */
+    char message[160];          /* error message of a failed request */
+} spg_request_info;
+
+spg_status spg_server_config_default(spg_server_config* config);
+spg_status spg_server_create(const spg_server_config* config, spg_server** server);
+/* Cancels queued requests, waits for running batches, frees undelivered results. */
+void spg_server_destroy(spg_server* server);
+/* Queues C = A * B; *ticket identifies it for spg_poll / spg_cancel. */
+spg_status spg_submit(spg_server* server, const spg_csr_view* A, const spg_csr_view* B, uint64_t* ticket);
+/* Waits up to wait_ms (< 0: without limit) for the request.  SPG_NOT_READY:
+ * still queued or running (poll again).  Otherwise the request is retired: its
+ * status is returned (SPG_OK with *C filled, the request's error, or
+ * SPG_CANCELLED) and `info` (may be NULL) describes it. */
+spg_status spg_poll(spg_server* server, uint64_t ticket, int32_t wait_ms, spg_csr_result* C,
+                    spg_request_info* info);
+/* Cancels a queued request (SPG_OK); SPG_NOT_READY if it is already running. */
+spg_status spg_cancel(spg_server* server, uint64_t ticket);
+/* Frees a result delivered by spg_poll. */
+spg_status spg_server_result_free(spg_server* server, spg_csr_result* C);
+
 /* ---- allocation-free product -------------------------------------------------
  * No counterpart in the reference: its multiply always allocates its result.
  * C = A * B for callers that cannot allocate memory when they multiply --

@@ -208,6 +208,7 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
 }
 
 // The phase pipeline for one or more products.  Results stay on the device.
+// products_out (optional) receives the scalar products of every product.
 void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevResult>& out, bool count_only,
                   int64_t* products_out) {
     cudaStream_t st = h->stream;
@@ -262,6 +263,14 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
     launch_bin_scatter(d_jobs, njobs, d_row_base, total_rows, d_ctrl->bin_off, d_ctrl->cursor, items, st);
     check_cuda(cudaGetLastError(), "K1 launch");
     cudaEventRecord(h->ev[1], st);
+    std::vector<int64_t> job_products(njobs, 0);
+    if (njobs > 1) {
+        int64_t* d_jp = ar.alloc<int64_t>(static_cast<size_t>(njobs), "job products");
+        launch_job_products(d_jobs, njobs, d_row_base, d_jp, st);
+        ++launches;
+        check_cuda(cudaMemcpyAsync(job_products.data(), d_jp, sizeof(int64_t) * njobs, cudaMemcpyDeviceToHost, st),
+                   "D2H job products");
+    }
     check_cuda(cudaMemcpyAsync(hc, d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, st), "D2H ctrl");
     sync(h);  // sync 1: bins and input checks
     if (hc->err.code) {
@@ -271,7 +280,8 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
     }
     const int64_t products = static_cast<int64_t>(hc->stats.products);
     const int64_t max_ub = static_cast<int64_t>(hc->stats.max_ub);
-    if (products_out) *products_out = products;
+    if (njobs == 1) job_products[0] = products;
+    if (products_out) std::copy(job_products.begin(), job_products.end(), products_out);
     if (count_only) {
         h->last = spg_timings{};
         h->last.products = products;
@@ -418,10 +428,7 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
         check_cuda(cudaGetLastError(), "rebase launch");
         sync(h);  // rb / idx host vectors must outlive the copies
     }
-    for (int j = 0; j < njobs; ++j) {
-        // per-product scalar products (for the FLOP count) are not split per job; report the batch total
-        out[j].products = njobs == 1 ? products : -1;
-    }
+    for (int j = 0; j < njobs; ++j) out[j].products = job_products[j];
     sync(h);
     h->last.ms_rowwork = elapsed(h->ev[0], h->ev[1]);
     h->last.ms_symbolic = elapsed(h->ev[1], h->ev[2]);
@@ -618,6 +625,18 @@ spg_status spg_scalar_multiplication_count(spg_handle* h, const spg_csr_view* A,
     return guarded(h, [&] {
         require(products != nullptr, SPG_INVALID_ARGUMENT, "products is NULL");
         std::vector<JobIn> in{{A, B, CsrView{}}};
+        std::vector<DevResult> out;
+        run_products(h, in, out, true, products);
+    });
+}
+
+spg_status spg_scalar_multiplication_count_batch(spg_handle* h, int32_t n, const spg_csr_view* A,
+                                                 const spg_csr_view* B, int64_t* products) {
+    return guarded(h, [&] {
+        require(n >= 0 && (n == 0 || (A && B && products)), SPG_INVALID_ARGUMENT, "bad batch arguments");
+        if (n == 0) return;
+        std::vector<JobIn> in(n);
+        for (int i = 0; i < n; ++i) in[i] = {&A[i], &B[i], CsrView{}};
         std::vector<DevResult> out;
         run_products(h, in, out, true, products);
     });

@@ -264,6 +264,25 @@ __global__ void gather_kernel(const int64_t* __restrict__ src, const int64_t* __
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[idx[i]];
 }
 
+// One CTA per product: its scalar products, the sum of its rows' ub.
+__global__ void job_products_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ job_row_base,
+                                    int64_t* __restrict__ out) {
+    __shared__ int64_t s_part[8];
+    const int j = blockIdx.x;
+    const int64_t rows = job_row_base[j + 1] - job_row_base[j];
+    const int64_t* ub = jobs[j].ub;
+    int64_t sum = 0;
+    for (int64_t r = threadIdx.x; r < rows; r += blockDim.x) sum += ub[r];
+    sum = warp_sum(sum);
+    if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = sum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int64_t t = 0;
+        for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) t += s_part[w];
+        out[j] = t;
+    }
+}
+
 // blockIdx.y selects the product; threads stride over its rows + 1 offsets.
 __global__ void rebase_kernel(const RebaseItem* __restrict__ items) {
     const RebaseItem it = items[blockIdx.y];
@@ -329,6 +348,12 @@ void launch_compact_holes(const Job* d_jobs, int njobs, const int64_t* d_job_row
 void launch_gather(const int64_t* d_src, const int64_t* d_idx, int64_t* d_dst, int n, cudaStream_t stream) {
     if (n <= 0) return;
     gather_kernel<<<grid_for(n, 256, 1024), 256, 0, stream>>>(d_src, d_idx, d_dst, n);
+}
+
+void launch_job_products(const Job* d_jobs, int njobs, const int64_t* d_job_row_base, int64_t* d_out,
+                         cudaStream_t stream) {
+    if (njobs <= 0) return;
+    job_products_kernel<<<njobs, 256, 0, stream>>>(d_jobs, d_job_row_base, d_out);
 }
 
 void launch_rebase(const RebaseItem* d_items, int n, int64_t max_rows, cudaStream_t stream) {

@@ -133,9 +133,13 @@ def library() -> C.CDLL:
         lib.spg_host_alloc.argtypes = [C.c_size_t]
         lib.spg_host_free.argtypes = [C.c_void_p]
         lib.spg_destroy.argtypes = [C.c_void_p]
+        lib.spg_server_destroy.argtypes = [C.c_void_p]
+        lib.spg_server_destroy.restype = None
         for name in ("spg_multiply", "spg_multiply_batch", "spg_accum_begin", "spg_accum_add", "spg_accum_finish",
                      "spg_result_download", "spg_result_free", "spg_scalar_multiplication_count",
-                     "spg_last_timings", "spg_create", "spg_config_default"):
+                     "spg_scalar_multiplication_count_batch", "spg_last_timings", "spg_create",
+                     "spg_config_default", "spg_server_create", "spg_submit", "spg_poll", "spg_cancel",
+                     "spg_server_result_free"):
             getattr(lib, name).restype = C.c_int
         _lib = lib
     return _lib
@@ -277,6 +281,15 @@ class Engine:
         self._check(lib.spg_accum_end(self.h))
         return DeviceResult(self, res) if loc == SPG_DEVICE else _take_host(res, self)
 
+    def scalar_multiplication_count_batch(self, pairs) -> list[int]:
+        keep: list = []
+        n = len(pairs)
+        A = (_View * max(n, 1))(*[_view(a, keep) for a, _ in pairs])
+        B = (_View * max(n, 1))(*[_view(b, keep) for _, b in pairs])
+        P = (C.c_int64 * max(n, 1))()
+        self._check(library().spg_scalar_multiplication_count_batch(self.h, C.c_int32(n), A, B, P))
+        return [int(P[i]) for i in range(n)]
+
     def scalar_multiplication_count(self, a, b) -> int:
         keep: list = []
         va, vb = _view(a, keep), _view(b, keep)
@@ -288,6 +301,130 @@ class Engine:
         t = Timings()
         self._check(library().spg_last_timings(self.h, C.byref(t)))
         return t.as_dict()
+
+
+class _ServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int32), ("lanes", C.c_int32), ("max_batch", C.c_int32), ("out_location", C.c_int32),
+                ("mode", C.c_int32), ("reserved", C.c_int32), ("hbm_budget_bytes", C.c_uint64),
+                ("max_batch_products", C.c_int64)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("queue_ms", C.c_double), ("service_ms", C.c_double), ("latency_ms", C.c_double),
+                ("products", C.c_int64), ("footprint_bytes", C.c_int64), ("batch_requests", C.c_int32),
+                ("lane", C.c_int32), ("batch_id", C.c_uint64), ("batch_launches", C.c_int64),
+                ("message", C.c_char * 160)]
+
+    def as_dict(self) -> dict:
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "message"}
+        d["message"] = self.message.decode(errors="replace")
+        return d
+
+
+class ServerResult:
+    """A result delivered by a Server (device or host memory owned by the library)."""
+
+    def __init__(self, server: "Server", res: _Result):
+        self._server = server
+        self._res = res
+        self.rows, self.cols, self.nnz, self.products = res.rows, res.cols, res.nnz, res.products
+        self.location = res.location
+
+    def download(self) -> Csr:
+        if self.location == SPG_HOST:
+            rp = np.ctypeslib.as_array(C.cast(self._res.row_ptr, C.POINTER(C.c_int64)), shape=(self.rows + 1,)).copy()
+            if self.nnz:
+                ci = np.ctypeslib.as_array(C.cast(self._res.col, C.POINTER(C.c_int32)), shape=(self.nnz,)).copy()
+                va = np.ctypeslib.as_array(C.cast(self._res.val, C.POINTER(C.c_double)), shape=(self.nnz,)).copy()
+            else:
+                ci, va = np.zeros(0, np.int32), np.zeros(0, np.float64)
+            return Csr(self.rows, self.cols, rp, ci, va)
+        eng = self._server._engine()
+        rp = np.empty(self.rows + 1, dtype=np.int64)
+        ci = np.empty(self.nnz, dtype=np.int32)
+        va = np.empty(self.nnz, dtype=np.float64)
+        eng._check(library().spg_result_download(
+            eng.h, C.byref(self._res), rp.ctypes.data_as(C.c_void_p),
+            ci.ctypes.data_as(C.c_void_p) if self.nnz else None, va.ctypes.data_as(C.c_void_p) if self.nnz else None))
+        return Csr(self.rows, self.cols, rp, ci, va)
+
+    def free(self):
+        if self._res is not None and self._server.s:
+            library().spg_server_result_free(self._server.s, C.byref(self._res))
+        self._res = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Server:
+    """Serving loop (spg_server_*): submit products as they arrive, poll for
+    results; batches of queued requests run together on `lanes` streams."""
+
+    def __init__(self, device: int = 0, lanes: int = 2, max_batch: int = 256, out: str = "device",
+                 mode: str = "auto", hbm_budget_bytes: int = 150 * 10**9, max_batch_products: int = 1 << 30):
+        lib = library()
+        cfg = _ServerConfig(device, lanes, max_batch, SPG_DEVICE if out == "device" else SPG_HOST, MODES[mode], 0,
+                            int(hbm_budget_bytes), int(max_batch_products))
+        s = C.c_void_p()
+        st = lib.spg_server_create(C.byref(cfg), C.byref(s))
+        if st != 0:
+            raise SpgError(st, "spg_server_create failed")
+        self.s = s
+        self.device = device
+        self._keep: dict = {}
+        self._eng = None
+
+    def _engine(self) -> Engine:
+        if self._eng is None:
+            self._eng = Engine(self.device)
+        return self._eng
+
+    def submit(self, a, b) -> int:
+        keep: list = []
+        va, vb = _view(a, keep), _view(b, keep)
+        t = C.c_uint64()
+        st = library().spg_submit(self.s, C.byref(va), C.byref(vb), C.byref(t))
+        if st != 0:
+            raise SpgError(st, "spg_submit failed")
+        self._keep[t.value] = (keep, a, b)
+        return t.value
+
+    def poll(self, ticket: int, wait_ms: int = -1):
+        """(status name, ServerResult or None, info dict); "SPG_NOT_READY" while it runs."""
+        res, info = _Result(), RequestInfo()
+        st = library().spg_poll(self.s, C.c_uint64(ticket), C.c_int32(wait_ms), C.byref(res), C.byref(info))
+        if st == 8:
+            return "SPG_NOT_READY", None, None
+        self._keep.pop(ticket, None)
+        return STATUS_NAMES.get(st, str(st)), (ServerResult(self, res) if st == 0 else None), info.as_dict()
+
+    def cancel(self, ticket: int) -> str:
+        return STATUS_NAMES.get(library().spg_cancel(self.s, C.c_uint64(ticket)), "?")
+
+    def close(self):
+        if getattr(self, "s", None):
+            library().spg_server_destroy(self.s)
+            self.s = None
+            self._keep.clear()
+        if getattr(self, "_eng", None) is not None:
+            self._eng.close()
+            self._eng = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ---------------------------------------------------------------------------
