@@ -85,8 +85,9 @@ typedef struct {
 typedef struct {
     float ms_rowwork, ms_symbolic, ms_scan, ms_numeric, ms_compact, ms_total;
     int64_t products, nnz, rows;
-    int64_t bin_rows[12];  /* rows per product-count bin (see spg_timings users) */
-    int64_t launches;  /* kernels this library launched for the call */
+    int64_t bin_rows[12];        /* rows per product-count bin: empty, <=32, <=64, ..., <=16384, heavier */
+    int64_t launches;            /* kernels this library launched for the call */
+    float ms_numeric_bin[12];    /* numeric-phase time of each bin (same order as bin_rows) */
 } spg_timings;
 
 typedef struct spg_handle spg_handle;

@@ -31,6 +31,7 @@ struct spg_handle {
     spg_config cfg{};
     std::string err;
     cudaEvent_t ev[6] = {};
+    cudaEvent_t bin_ev[kNumBins] = {};  // end of each bin's numeric launch
     spg_timings last{};
     // accumulate mode: the running sum S (device result) and its shape
     bool acc_active = false;
@@ -337,9 +338,11 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
         jobs[j].holes = exact ? 0 : 1;
     }
     check_cuda(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(Job) * njobs, cudaMemcpyHostToDevice, st), "H2D jobs");
-    for (int b = 1; b < kNumBins; ++b)
+    for (int b = 1; b < kNumBins; ++b) {
         launch_numeric(b, d_jobs, items + bin_off[b], bin_count[b], max_ub, scratch, scratch_bytes, &d_ctrl->stats,
                        &d_ctrl->err, st, h->num_sms);
+        cudaEventRecord(h->bin_ev[b], st);
+    }
     check_cuda(cudaGetLastError(), "K4 launch");
     cudaEventRecord(h->ev[4], st);
     check_cuda(cudaMemcpyAsync(hc, d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, st), "D2H ctrl");
@@ -436,6 +439,9 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
     h->last.ms_numeric = elapsed(h->ev[3], h->ev[4]);
     h->last.ms_compact = elapsed(h->ev[4], h->ev[5]);
     h->last.ms_total = elapsed(h->ev[0], h->ev[5]);
+    h->last.ms_numeric_bin[0] = 0.0f;
+    for (int b = 1; b < kNumBins; ++b)
+        h->last.ms_numeric_bin[b] = elapsed(b == 1 ? h->ev[3] : h->bin_ev[b - 1], h->bin_ev[b]);
     h->last.products = products;
     h->last.nnz = nz_total;
     h->last.rows = total_rows;
@@ -548,6 +554,7 @@ spg_status spg_create(const spg_config* config, spg_handle** out) {
     }
     cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
     for (auto& e : h->ev) cudaEventCreate(&e);
+    for (auto& e : h->bin_ev) cudaEventCreate(&e);
     cudaMemPool_t pool;
     if (cudaDeviceGetDefaultMemPool(&pool, h->device) == cudaSuccess) {
         uint64_t threshold = UINT64_MAX;
@@ -563,6 +570,7 @@ void spg_destroy(spg_handle* h) {
     if (h->acc_has) free_result_arrays(h, &h->acc);
     cudaStreamSynchronize(h->stream);
     for (auto& e : h->ev) cudaEventDestroy(e);
+    for (auto& e : h->bin_ev) cudaEventDestroy(e);
     cudaStreamDestroy(h->stream);
     cudaFreeHost(h->ctrl);
     delete h;

@@ -101,11 +101,12 @@ class Timings(C.Structure):
     _fields_ = [("ms_rowwork", C.c_float), ("ms_symbolic", C.c_float), ("ms_scan", C.c_float),
                 ("ms_numeric", C.c_float), ("ms_compact", C.c_float), ("ms_total", C.c_float),
                 ("products", C.c_int64), ("nnz", C.c_int64), ("rows", C.c_int64), ("bin_rows", C.c_int64 * 12),
-                ("launches", C.c_int64)]
+                ("launches", C.c_int64), ("ms_numeric_bin", C.c_float * 12)]
 
     def as_dict(self) -> dict:
-        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "bin_rows"}
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k not in ("bin_rows", "ms_numeric_bin")}
         d["bin_rows"] = {BIN_NAMES[i]: int(self.bin_rows[i]) for i in range(len(BIN_NAMES))}
+        d["ms_numeric_bin"] = {BIN_NAMES[i]: float(self.ms_numeric_bin[i]) for i in range(len(BIN_NAMES))}
         return d
 
 
