@@ -34,6 +34,17 @@ __device__ inline void row_sync() {
 
 constexpr int log2_ceil_c(int x) { return x <= 1 ? 0 : 1 + log2_ceil_c((x + 1) / 2); }
 
+// Digit counters of W warps: counter (digit d, warp w) lives at hidx<W>(d, w),
+// digit-major with one padding word after every W counters.  (W + 1) is odd, so
+// the counters that one warp's lanes touch for different digits fall in
+// different banks; without the padding they would share 32 / W banks.
+template <int W>
+constexpr int kHistWords = W == 1 ? 256 : 256 * (W + 1);
+template <int W>
+__device__ __forceinline__ int hidx(int d, int w) {
+    return W == 1 ? d : d * (W + 1) + w;
+}
+
 // SV: product values in shared memory (else in a per-CTA global slab).
 template <int W, int ITEMS, bool SV = true>
 struct RowSmem {
@@ -43,25 +54,27 @@ struct RowSmem {
     SegTab<W * 32, int32_t> seg;  // enumeration batch
     int64_t warp_tmp[W + 1];    // block scans
     uint32_t keys[kCap];        // columns (unpacked) or packed (column, sequence) words
-    uint32_t hist[256 * W];     // digit counters, digit-major
+    uint32_t hist[kHistWords<W>];  // digit counters at hidx<W>(digit, warp)
     uint32_t cnt[W * ITEMS];    // kept entries per (warp, item)
     uint16_t seqs[kCap];        // sequence numbers of the unpacked path
     int32_t red[2 * W];         // min / max column reduction
     uint32_t kept;              // stored entries of the row (upper-bound mode)
 };
 
-// Exclusive scan of the 256*W digit counters, 8 consecutive counters per thread.
+// Exclusive scan of the 256*W digit counters in (digit, warp) order, 8
+// consecutive counters per thread (logical index L lives at L + L / W).
 template <int W>
 __device__ inline void scan_counters(uint32_t* c, int64_t* tmp) {
     constexpr int kPer = 8;
     const int lane = threadIdx.x & 31;
     const int warp = W == 1 ? 0 : (threadIdx.x >> 5);
     const int tid = W == 1 ? lane : threadIdx.x;
+    auto phys = [](int L) { return W == 1 ? L : L + L / W; };
     uint32_t v[kPer];
     uint32_t sum = 0;
 #pragma unroll
     for (int j = 0; j < kPer; ++j) {
-        v[j] = c[tid * kPer + j];
+        v[j] = c[phys(tid * kPer + j)];
         sum += v[j];
     }
     const uint32_t incl = warp_incl_scan(sum, lane);
@@ -79,7 +92,7 @@ __device__ inline void scan_counters(uint32_t* c, int64_t* tmp) {
     }
 #pragma unroll
     for (int j = 0; j < kPer; ++j) {
-        c[tid * kPer + j] = base;
+        c[phys(tid * kPer + j)] = base;
         base += v[j];
     }
 }
@@ -161,7 +174,7 @@ __device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double*
         // Packed words (col - cmin) << kSeqBits | seq; the first pass packs.
         for (int shift = 0; shift < nbits || shift == 0; shift += 8) {
             uint32_t k[ITEMS], rk[ITEMS];
-            for (int d = tid; d < 256 * W; d += W * 32) sm.hist[d] = 0;
+            for (int d = tid; d < kHistWords<W>; d += W * 32) sm.hist[d] = 0;
             row_sync<W>();
 #pragma unroll
             for (int i = 0; i < ITEMS; ++i) {
@@ -173,7 +186,7 @@ __device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double*
                     k[i] = shift == 0 ? ((raw - cmin) << kSeqBits) | static_cast<uint32_t>(pos) : raw;
                     d = (k[i] >> (kSeqBits + shift)) & 255u;
                 }
-                rk[i] = rank_item(d, &sm.hist[d * W + warp], lane);
+                rk[i] = rank_item(d, &sm.hist[hidx<W>(d, warp)], lane);
             }
             if (nbits == 0) {  // one column: already in sequence order; just pack
                 row_sync<W>();
@@ -195,7 +208,7 @@ __device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double*
                 const int pos = (warp * ITEMS + i) * 32 + lane;
                 if (pos < P) {
                     const uint32_t d = (k[i] >> (kSeqBits + shift)) & 255u;
-                    sm.keys[sm.hist[d * W + warp] + rk[i]] = k[i];
+                    sm.keys[sm.hist[hidx<W>(d, warp)] + rk[i]] = k[i];
                 }
             }
             row_sync<W>();
@@ -206,7 +219,7 @@ __device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double*
         for (int shift = 0; shift < nbits; shift += 8) {
             uint32_t k[ITEMS], rk[ITEMS];
             uint16_t s[ITEMS];
-            for (int d = tid; d < 256 * W; d += W * 32) sm.hist[d] = 0;
+            for (int d = tid; d < kHistWords<W>; d += W * 32) sm.hist[d] = 0;
             row_sync<W>();
 #pragma unroll
             for (int i = 0; i < ITEMS; ++i) {
@@ -215,7 +228,7 @@ __device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double*
                 k[i] = valid ? sm.keys[pos] : 0u;
                 s[i] = valid ? sm.seqs[pos] : uint16_t{0};
                 const uint32_t d = valid ? (((k[i] - cmin) >> shift) & 255u) : 255u;
-                rk[i] = rank_item(d, &sm.hist[d * W + warp], lane);
+                rk[i] = rank_item(d, &sm.hist[hidx<W>(d, warp)], lane);
             }
             row_sync<W>();
             scan_counters<W>(sm.hist, sm.warp_tmp);
@@ -224,7 +237,7 @@ __device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double*
             for (int i = 0; i < ITEMS; ++i) {
                 const int pos = (warp * ITEMS + i) * 32 + lane;
                 const uint32_t d = pos < P ? (((k[i] - cmin) >> shift) & 255u) : 255u;
-                const uint32_t dst = sm.hist[d * W + warp] + rk[i];
+                const uint32_t dst = sm.hist[hidx<W>(d, warp)] + rk[i];
                 if (dst < static_cast<uint32_t>(P)) {
                     sm.keys[dst] = k[i];
                     sm.seqs[dst] = s[i];
@@ -433,7 +446,7 @@ constexpr int kHeavyTile = kHeavyThreads * kHeavyItems;
 struct HeavySmem {
     SegTab<kHeavyThreads> seg;
     int64_t warp_tmp[kHeavyW + 1];
-    uint32_t hist[256 * kHeavyW];
+    uint32_t hist[kHistWords<kHeavyW>];
     uint32_t digit_base[256];
     uint32_t digit_tot[256];
     uint32_t cnt[kHeavyW * kHeavyItems];
@@ -535,7 +548,7 @@ num_heavy_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items
             for (int64_t t = 0; t < ntiles; ++t) {
                 const int64_t tile0 = t * kHeavyTile;
                 uint32_t k[kHeavyItems], s[kHeavyItems], rk[kHeavyItems];
-                for (int d = tid; d < 256 * kHeavyW; d += kHeavyThreads) sm.hist[d] = 0;
+                for (int d = tid; d < kHistWords<kHeavyW>; d += kHeavyThreads) sm.hist[d] = 0;
                 __syncthreads();
 #pragma unroll
                 for (int i = 0; i < kHeavyItems; ++i) {
@@ -544,13 +557,13 @@ num_heavy_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items
                     k[i] = valid ? kin[pos] : 0u;
                     s[i] = valid ? sin[pos] : 0u;
                     const uint32_t d = valid ? (((k[i] - cmin) >> shift) & 255u) : 255u;
-                    rk[i] = rank_item(d, &sm.hist[d * kHeavyW + warp], lane);
+                    rk[i] = rank_item(d, &sm.hist[hidx<kHeavyW>(d, warp)], lane);
                 }
                 __syncthreads();
                 if (tid < 256) {  // this tile's count of digit tid
                     uint32_t c = 0;
 #pragma unroll
-                    for (int w = 0; w < kHeavyW; ++w) c += sm.hist[tid * kHeavyW + w];
+                    for (int w = 0; w < kHeavyW; ++w) c += sm.hist[hidx<kHeavyW>(tid, w)];
                     sm.digit_tot[tid] = c;
                 }
                 __syncthreads();
@@ -562,7 +575,7 @@ num_heavy_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items
                     if (pos < P) {
                         const uint32_t d = ((k[i] - cmin) >> shift) & 255u;
                         // position among this tile's items of digit d, then the row-wide base
-                        const uint32_t within = sm.hist[d * kHeavyW + warp] + rk[i] - sm.hist[d * kHeavyW];
+                        const uint32_t within = sm.hist[hidx<kHeavyW>(d, warp)] + rk[i] - sm.hist[hidx<kHeavyW>(d, 0)];
                         const uint32_t dst = sm.digit_base[d] + within;
                         kout[dst] = k[i];
                         sout[dst] = s[i];
