@@ -54,7 +54,9 @@ struct RowSmem {
     SegTab<W * 32, int32_t> seg;  // enumeration batch
     int64_t warp_tmp[W + 1];    // block scans
     uint32_t keys[kCap];        // columns (unpacked) or packed (column, sequence) words
-    uint32_t hist[kHistWords<W>];  // digit counters at hidx<W>(digit, warp)
+    uint32_t hist[W == 1 ? 1 : 2][kHistWords<W>];  // digit counters at hidx<W>(digit, warp); CTA rows
+                                                   // alternate two sets so that clearing the next
+                                                   // pass's set needs no barrier of its own
     uint32_t cnt[W * ITEMS];    // kept entries per (warp, item)
     uint16_t seqs[kCap];        // sequence numbers of the unpacked path
     int32_t red[2 * W];         // min / max column reduction
@@ -79,16 +81,11 @@ __device__ inline void scan_counters(uint32_t* c, int64_t* tmp) {
     }
     const uint32_t incl = warp_incl_scan(sum, lane);
     uint32_t base = incl - sum;
-    if (W > 1) {
+    if (W > 1) {  // every warp scans the W warp totals itself: one barrier
         if (lane == 31) tmp[warp] = incl;
         __syncthreads();
-        if (warp == 0) {
-            const uint32_t w = lane < W ? static_cast<uint32_t>(tmp[lane]) : 0u;
-            const uint32_t wi = warp_incl_scan(w, lane);
-            if (lane < W) tmp[lane] = wi - w;
-        }
-        __syncthreads();
-        base += static_cast<uint32_t>(tmp[warp]);
+        const uint32_t t = lane < W ? static_cast<uint32_t>(tmp[lane]) : 0u;
+        base += __shfl_sync(0xffffffffu, warp_incl_scan(t, lane) - t, warp);
     }
 #pragma unroll
     for (int j = 0; j < kPer; ++j) {
@@ -170,12 +167,17 @@ __device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double*
     using Sm = RowSmem<W, ITEMS, SV>;
     constexpr int kSeqBits = Sm::kSeqBits;
     // 2. stable LSD radix sort by column
+    int hb = 0;  // counter set of this pass
+    auto clear_next = [&](int set) {
+        for (int d = tid; d < kHistWords<W>; d += W * 32) sm.hist[set][d] = 0;
+    };
+    clear_next(0);
+    row_sync<W>();
     if constexpr (PACKED) {
         // Packed words (col - cmin) << kSeqBits | seq; the first pass packs.
         for (int shift = 0; shift < nbits || shift == 0; shift += 8) {
             uint32_t k[ITEMS], rk[ITEMS];
-            for (int d = tid; d < kHistWords<W>; d += W * 32) sm.hist[d] = 0;
-            row_sync<W>();
+            uint32_t* hist = sm.hist[hb];
 #pragma unroll
             for (int i = 0; i < ITEMS; ++i) {
                 const int pos = (warp * ITEMS + i) * 32 + lane;
@@ -186,7 +188,7 @@ __device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double*
                     k[i] = shift == 0 ? ((raw - cmin) << kSeqBits) | static_cast<uint32_t>(pos) : raw;
                     d = (k[i] >> (kSeqBits + shift)) & 255u;
                 }
-                rk[i] = rank_item(d, &sm.hist[hidx<W>(d, warp)], lane);
+                rk[i] = rank_item(d, &hist[hidx<W>(d, warp)], lane);
             }
             if (nbits == 0) {  // one column: already in sequence order; just pack
                 row_sync<W>();
@@ -199,7 +201,7 @@ __device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double*
                 break;
             }
             row_sync<W>();
-            scan_counters<W>(sm.hist, sm.warp_tmp);
+            scan_counters<W>(hist, sm.warp_tmp);
             row_sync<W>();
 #pragma unroll
             for (int i = 0; i < ITEMS; ++i) {
@@ -208,8 +210,15 @@ __device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double*
                 const int pos = (warp * ITEMS + i) * 32 + lane;
                 if (pos < P) {
                     const uint32_t d = (k[i] >> (kSeqBits + shift)) & 255u;
-                    sm.keys[sm.hist[hidx<W>(d, warp)] + rk[i]] = k[i];
+                    sm.keys[hist[hidx<W>(d, warp)] + rk[i]] = k[i];
                 }
+            }
+            if constexpr (W == 1) {
+                __syncwarp();
+                clear_next(0);
+            } else {
+                clear_next(hb ^ 1);
+                hb ^= 1;
             }
             row_sync<W>();
         }
@@ -219,8 +228,7 @@ __device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double*
         for (int shift = 0; shift < nbits; shift += 8) {
             uint32_t k[ITEMS], rk[ITEMS];
             uint16_t s[ITEMS];
-            for (int d = tid; d < kHistWords<W>; d += W * 32) sm.hist[d] = 0;
-            row_sync<W>();
+            uint32_t* hist = sm.hist[hb];
 #pragma unroll
             for (int i = 0; i < ITEMS; ++i) {
                 const int pos = (warp * ITEMS + i) * 32 + lane;
@@ -228,20 +236,27 @@ __device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double*
                 k[i] = valid ? sm.keys[pos] : 0u;
                 s[i] = valid ? sm.seqs[pos] : uint16_t{0};
                 const uint32_t d = valid ? (((k[i] - cmin) >> shift) & 255u) : 255u;
-                rk[i] = rank_item(d, &sm.hist[hidx<W>(d, warp)], lane);
+                rk[i] = rank_item(d, &hist[hidx<W>(d, warp)], lane);
             }
             row_sync<W>();
-            scan_counters<W>(sm.hist, sm.warp_tmp);
+            scan_counters<W>(hist, sm.warp_tmp);
             row_sync<W>();
 #pragma unroll
             for (int i = 0; i < ITEMS; ++i) {
                 const int pos = (warp * ITEMS + i) * 32 + lane;
                 const uint32_t d = pos < P ? (((k[i] - cmin) >> shift) & 255u) : 255u;
-                const uint32_t dst = sm.hist[hidx<W>(d, warp)] + rk[i];
+                const uint32_t dst = hist[hidx<W>(d, warp)] + rk[i];
                 if (dst < static_cast<uint32_t>(P)) {
                     sm.keys[dst] = k[i];
                     sm.seqs[dst] = s[i];
                 }
+            }
+            if constexpr (W == 1) {
+                __syncwarp();
+                clear_next(0);
+            } else {
+                clear_next(hb ^ 1);
+                hb ^= 1;
             }
             row_sync<W>();
         }
