@@ -85,9 +85,10 @@ typedef struct {
 typedef struct {
     float ms_rowwork, ms_symbolic, ms_scan, ms_numeric, ms_compact, ms_total;
     int64_t products, nnz, rows;
-    int64_t bin_rows[12];        /* rows per product-count bin: empty, <=32, <=64, ..., <=16384, heavier */
+    int64_t bin_rows[20];        /* rows per product-count bin: empty, <=32, 64, 96, 128, 192, 256, 384, 512,
+                                    768, 1024, 1536, 2048, 3072, 4096, 6144, 8192, 12288, 16384, heavier */
     int64_t launches;            /* kernels this library launched for the call */
-    float ms_numeric_bin[12];    /* numeric-phase time of each bin (same order as bin_rows) */
+    float ms_numeric_bin[20];    /* numeric-phase time of each bin (same order as bin_rows) */
 } spg_timings;
 
 typedef struct spg_handle spg_handle;

@@ -339,6 +339,7 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
     }
     check_cuda(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(Job) * njobs, cudaMemcpyHostToDevice, st), "H2D jobs");
     for (int b = 1; b < kNumBins; ++b) {
+        if (!bin_count[b]) continue;
         launch_numeric(b, d_jobs, items + bin_off[b], bin_count[b], max_ub, scratch, scratch_bytes, &d_ctrl->stats,
                        &d_ctrl->err, st, h->num_sms);
         cudaEventRecord(h->bin_ev[b], st);
@@ -439,9 +440,13 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
     h->last.ms_numeric = elapsed(h->ev[3], h->ev[4]);
     h->last.ms_compact = elapsed(h->ev[4], h->ev[5]);
     h->last.ms_total = elapsed(h->ev[0], h->ev[5]);
-    h->last.ms_numeric_bin[0] = 0.0f;
-    for (int b = 1; b < kNumBins; ++b)
-        h->last.ms_numeric_bin[b] = elapsed(b == 1 ? h->ev[3] : h->bin_ev[b - 1], h->bin_ev[b]);
+    cudaEvent_t prev = h->ev[3];
+    for (int b = 0; b < kNumBins; ++b) {
+        h->last.ms_numeric_bin[b] = 0.0f;
+        if (b == kBinEmpty || !bin_count[b]) continue;
+        h->last.ms_numeric_bin[b] = elapsed(prev, h->bin_ev[b]);
+        prev = h->bin_ev[b];
+    }
     h->last.products = products;
     h->last.nnz = nz_total;
     h->last.rows = total_rows;

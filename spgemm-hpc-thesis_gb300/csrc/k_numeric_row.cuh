@@ -1,0 +1,484 @@
+// K4 numeric phase: every output row sorted, summed and written without zeros.
+//
+// For a row with P products the kernel
+//   1. enumerates the products in reference order (spg_enum.cuh): product t gets
+//      its column, sequence number t and value __dmul_rn(a, b) (one rounding, as
+//      `const double product = aValue * b` in spgemm_exchange.cpp:287);
+//   2. sorts the products by column with a stable LSD radix sort (8-bit digits
+//      over the bits of max(col) - min(col) only; ranks from ballot-matched
+//      lane groups and per-warp digit counters), so that equal columns stay in
+//      product order.
+//      When the column range and the sequence number fit in 32 bits together,
+//      the sort moves one packed word (column - min) << s | seq per product;
+//      otherwise it moves the column and a 16-bit sequence number side by side;
+//   3. sums each run of equal columns sequentially in product order with
+//      __dadd_rn, starting from its first product (the `emplace` then `+=` of
+//      spgemm_exchange.cpp:288-293), and keeps the sums that are != 0.0
+//      (spgemm_exchange.cpp:304; NaN and infinities are kept);
+//   4. writes the kept (column, sum) pairs, already in column order, at the
+//      row's output offset (job.cnt[row]) and the kept count into job.nz[row].
+// Every coordinate is therefore bit-identical to the serial reference.  Rows of
+// <= 512 products run one per warp (num_warp_kernel), rows of <= 8192 one per
+// CTA with everything in shared memory, rows of <= 16384 one per CTA with the
+// product values in a global slab (num_block_kernel); heavier rows run one per
+// CTA with the whole sort in a global slab (num_heavy_kernel, k_numeric.cu).
+#pragma once
+
+#include "spg_enum.cuh"
+
+namespace spg {
+namespace {
+
+template <int W>
+__device__ inline void row_sync() {
+    if (W == 1) __syncwarp();
+    else __syncthreads();
+}
+
+constexpr int log2_ceil_c(int x) { return x <= 1 ? 0 : 1 + log2_ceil_c((x + 1) / 2); }
+
+// Digit counters of W warps: counter (digit d, warp w) lives at hidx<W>(d, w),
+// digit-major with one padding word after every W counters.  (W + 1) is odd, so
+// the counters that one warp's lanes touch for different digits fall in
+// different banks; without the padding they would share 32 / W banks.
+template <int W>
+constexpr int kHistWords = W == 1 ? 256 : 256 * (W + 1);
+template <int W>
+__device__ __forceinline__ int hidx(int d, int w) {
+    return W == 1 ? d : d * (W + 1) + w;
+}
+
+// SV: product values in shared memory (else in a per-CTA global slab).
+template <int W, int ITEMS, bool SV = true>
+struct RowSmem {
+    static constexpr int kCap = W * 32 * ITEMS;
+    static constexpr int kSeqBits = log2_ceil_c(kCap);
+    double vals[SV ? kCap : 1];  // product values by sequence number; run sums in place
+    SegTab<W * 32, int32_t> seg;  // enumeration batch
+    int64_t warp_tmp[W + 1];    // block scans
+    uint32_t keys[kCap];        // columns (unpacked) or packed (column, sequence) words
+    uint32_t hist[W == 1 ? 1 : 2][kHistWords<W>];  // digit counters at hidx<W>(digit, warp); CTA rows
+                                                   // alternate two sets so that clearing the next
+                                                   // pass's set needs no barrier of its own
+    uint32_t cnt[W * ITEMS];    // kept entries per (warp, item)
+    uint16_t seqs[kCap];        // sequence numbers of the unpacked path
+    int32_t red[2 * W];         // min / max column reduction
+    uint32_t kept;              // stored entries of the row (upper-bound mode)
+};
+
+// Exclusive scan of the 256*W digit counters in (digit, warp) order, 8
+// consecutive counters per thread (logical index L lives at L + L / W).
+template <int W>
+__device__ inline void scan_counters(uint32_t* c, int64_t* tmp) {
+    constexpr int kPer = 8;
+    const int lane = threadIdx.x & 31;
+    const int warp = W == 1 ? 0 : (threadIdx.x >> 5);
+    const int tid = W == 1 ? lane : threadIdx.x;
+    auto phys = [](int L) { return W == 1 ? L : L + L / W; };
+    uint32_t v[kPer];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+        v[j] = c[phys(tid * kPer + j)];
+        sum += v[j];
+    }
+    const uint32_t incl = warp_incl_scan(sum, lane);
+    uint32_t base = incl - sum;
+    if (W > 1) {  // every warp scans the W warp totals itself: one barrier
+        if (lane == 31) tmp[warp] = incl;
+        __syncthreads();
+        const uint32_t t = lane < W ? static_cast<uint32_t>(tmp[lane]) : 0u;
+        base += __shfl_sync(0xffffffffu, warp_incl_scan(t, lane) - t, warp);
+    }
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+        c[phys(tid * kPer + j)] = base;
+        base += v[j];
+    }
+}
+
+// Lanes of the warp holding the same 8-bit digit: the intersection of one
+// ballot per digit bit (a ballot for each set bit, its complement for each
+// clear bit).  Eight votes cost a fraction of one __match_any_sync on GB300.
+__device__ inline unsigned digit_peers(uint32_t d) {
+    unsigned peers = 0xffffffffu;
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+        const unsigned bit = (d >> b) & 1u;
+        const unsigned set = __ballot_sync(0xffffffffu, bit);
+        peers &= set ^ (bit - 1u);  // set where this lane's bit is 1, ~set where it is 0
+    }
+    return peers;
+}
+
+// Stable rank of one striped item against this warp's digit counters: the
+// group of lanes holding the same digit (digit_peers); its first lane advances
+// the counter by the group size (one shared atomic) and broadcasts the old
+// value.  Items of a warp are ranked in order, so ranks follow
+// (warp, item, lane) order.
+__device__ inline uint32_t rank_item(uint32_t d, uint32_t* counter_of_d, int lane) {
+    const unsigned peers = digit_peers(d);
+    const int leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter_of_d, static_cast<uint32_t>(__popc(peers)));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    return base + __popc(peers & lanemask_lt());
+}
+
+// Exclusive scan of the W*ITEMS per-(warp, item) kept counts by warp 0; the
+// total goes to red[0].
+template <int W, int ITEMS>
+__device__ inline void scan_kept(uint32_t* cnt, int32_t* red, int warp, int lane) {
+    constexpr int kN = W * ITEMS;
+    constexpr int kPer = (kN + 31) / 32;
+    if (warp == 0) {
+        uint32_t v[kPer];
+        uint32_t tot = 0;
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            const int idx = lane * kPer + j;
+            v[j] = idx < kN ? cnt[idx] : 0u;
+            tot += v[j];
+        }
+        const uint32_t incl = warp_incl_scan(tot, lane);
+        uint32_t base = incl - tot;
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            const int idx = lane * kPer + j;
+            if (idx < kN) cnt[idx] = base;
+            base += v[j];
+        }
+        if (lane == 31) red[0] = static_cast<int32_t>(incl);
+    }
+}
+
+// Where a row's result goes, read once from the Job (locals, not reloaded
+// through the Job reference after every global store).
+struct RowOut {
+    int32_t* __restrict__ c_col;
+    double* __restrict__ c_val;
+    int64_t out0;       // first slot of the row in C_tmp
+    int64_t* nz;        // the row's stored-entry count
+    int32_t holes;      // upper-bound mode: slot-per-position output with holes
+};
+
+// Steps 2-4 of a row for one key layout (PACKED: (col - cmin) << kSeqBits | seq
+// words; otherwise columns and 16-bit sequence numbers).
+template <int W, int ITEMS, bool SV, bool PACKED>
+__device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double* vals, int P, uint32_t cmin,
+                           int nbits, int lane, int warp, int tid) {
+    using Sm = RowSmem<W, ITEMS, SV>;
+    constexpr int kSeqBits = Sm::kSeqBits;
+    // 2. stable LSD radix sort by column
+    int hb = 0;  // counter set of this pass
+    auto clear_next = [&](int set) {
+        for (int d = tid; d < kHistWords<W>; d += W * 32) sm.hist[set][d] = 0;
+    };
+    clear_next(0);
+    row_sync<W>();
+    if constexpr (PACKED) {
+        // Packed words (col - cmin) << kSeqBits | seq; the first pass packs.
+        for (int shift = 0; shift < nbits || shift == 0; shift += 8) {
+            uint32_t k[ITEMS], rk[ITEMS];
+            uint32_t* hist = sm.hist[hb];
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) {
+                const int pos = (warp * ITEMS + i) * 32 + lane;
+                uint32_t d = 255u;
+                k[i] = 0xffffffffu;
+                if (pos < P) {
+                    const uint32_t raw = sm.keys[pos];
+                    k[i] = shift == 0 ? ((raw - cmin) << kSeqBits) | static_cast<uint32_t>(pos) : raw;
+                    d = (k[i] >> (kSeqBits + shift)) & 255u;
+                }
+                rk[i] = rank_item(d, &hist[hidx<W>(d, warp)], lane);
+            }
+            if (nbits == 0) {  // one column: already in sequence order; just pack
+                row_sync<W>();
+#pragma unroll
+                for (int i = 0; i < ITEMS; ++i) {
+                    const int pos = (warp * ITEMS + i) * 32 + lane;
+                    if (pos < P) sm.keys[pos] = k[i];
+                }
+                row_sync<W>();
+                break;
+            }
+            row_sync<W>();
+            scan_counters<W>(hist, sm.warp_tmp);
+            row_sync<W>();
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) {
+                // Padding items were ranked under digit 255; a recomputed digit of
+                // 0xffffffff is not 255 once fewer than 8 key bits remain.
+                const int pos = (warp * ITEMS + i) * 32 + lane;
+                if (pos < P) {
+                    const uint32_t d = (k[i] >> (kSeqBits + shift)) & 255u;
+                    sm.keys[hist[hidx<W>(d, warp)] + rk[i]] = k[i];
+                }
+            }
+            if constexpr (W == 1) {
+                __syncwarp();
+                clear_next(0);
+            } else {
+                clear_next(hb ^ 1);
+                hb ^= 1;
+            }
+            row_sync<W>();
+        }
+    } else {
+        for (int i = tid; i < P; i += W * 32) sm.seqs[i] = static_cast<uint16_t>(i);
+        row_sync<W>();
+        for (int shift = 0; shift < nbits; shift += 8) {
+            uint32_t k[ITEMS], rk[ITEMS];
+            uint16_t s[ITEMS];
+            uint32_t* hist = sm.hist[hb];
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) {
+                const int pos = (warp * ITEMS + i) * 32 + lane;
+                const bool valid = pos < P;
+                k[i] = valid ? sm.keys[pos] : 0u;
+                s[i] = valid ? sm.seqs[pos] : uint16_t{0};
+                const uint32_t d = valid ? (((k[i] - cmin) >> shift) & 255u) : 255u;
+                rk[i] = rank_item(d, &hist[hidx<W>(d, warp)], lane);
+            }
+            row_sync<W>();
+            scan_counters<W>(hist, sm.warp_tmp);
+            row_sync<W>();
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) {
+                const int pos = (warp * ITEMS + i) * 32 + lane;
+                const uint32_t d = pos < P ? (((k[i] - cmin) >> shift) & 255u) : 255u;
+                const uint32_t dst = hist[hidx<W>(d, warp)] + rk[i];
+                if (dst < static_cast<uint32_t>(P)) {
+                    sm.keys[dst] = k[i];
+                    sm.seqs[dst] = s[i];
+                }
+            }
+            if constexpr (W == 1) {
+                __syncwarp();
+                clear_next(0);
+            } else {
+                clear_next(hb ^ 1);
+                hb ^= 1;
+            }
+            row_sync<W>();
+        }
+    }
+
+    // Column and sequence number of sorted position pos.
+    auto col_at = [&](int pos) -> uint32_t {
+        return PACKED ? (sm.keys[pos] >> kSeqBits) : sm.keys[pos] - cmin;
+    };
+    auto seq_at = [&](int pos) -> uint32_t {
+        return PACKED ? (sm.keys[pos] & ((1u << kSeqBits) - 1u)) : sm.seqs[pos];
+    };
+
+    if (out.holes) {
+        // 3+4 in one pass (upper-bound mode): sorted position pos owns slot
+        // out0 + pos of the row's reserved range; the first position of every run
+        // writes (column, sum) when the sum is != 0, every other slot column -1.
+        const int64_t out0 = out.out0;
+        uint32_t kept = 0;
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i) {
+            const int pos = (warp * ITEMS + i) * 32 + lane;
+            if (pos < P) {
+                const uint32_t c = col_at(pos);
+                int32_t oc = -1;
+                double acc = 0.0;
+                if (pos == 0 || col_at(pos - 1) != c) {
+                    acc = vals[seq_at(pos)];
+                    for (int q = pos + 1; q < P && col_at(q) == c; ++q) acc = __dadd_rn(acc, vals[seq_at(q)]);
+                    if (acc != 0.0) {
+                        oc = static_cast<int32_t>(c + cmin);
+                        ++kept;
+                    }
+                }
+                out.c_col[out0 + pos] = oc;
+                if (oc >= 0) out.c_val[out0 + pos] = acc;
+            }
+        }
+        kept = warp_sum(kept);
+        if (W == 1) {
+            if (lane == 0) *out.nz = kept;
+        } else {
+            if (lane == 0) atomicAdd(&sm.kept, kept);
+            __syncthreads();
+            if (tid == 0) *out.nz = sm.kept;
+        }
+        row_sync<W>();
+        return;
+    }
+
+    // 3. runs of equal columns summed in product order; each run's sum is stored
+    //    in place of its first product's value
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+        const int pos = (warp * ITEMS + i) * 32 + lane;
+        bool keep = false;
+        if (pos < P) {
+            const uint32_t c = col_at(pos);
+            if (pos == 0 || col_at(pos - 1) != c) {
+                const uint32_t s0 = seq_at(pos);
+                double acc = vals[s0];
+                for (int q = pos + 1; q < P && col_at(q) == c; ++q) acc = __dadd_rn(acc, vals[seq_at(q)]);
+                vals[s0] = acc;
+                keep = acc != 0.0;
+            }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (lane == 0) sm.cnt[warp * ITEMS + i] = __popc(m);
+    }
+    row_sync<W>();
+    scan_kept<W, ITEMS>(sm.cnt, sm.red, warp, lane);
+    row_sync<W>();
+
+    // 4. kept (column, sum) pairs in sorted order
+    const int64_t out0 = out.out0;
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+        const int pos = (warp * ITEMS + i) * 32 + lane;
+        bool keep = false;
+        uint32_t c = 0;
+        double v = 0.0;
+        if (pos < P) {
+            c = col_at(pos);
+            if (pos == 0 || col_at(pos - 1) != c) {
+                v = vals[seq_at(pos)];
+                keep = v != 0.0;
+            }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (keep) {
+            const int64_t idx = out0 + sm.cnt[warp * ITEMS + i] + __popc(m & lanemask_lt());
+            out.c_col[idx] = static_cast<int32_t>(c + cmin);
+            out.c_val[idx] = v;
+        }
+    }
+    if (tid == 0) *out.nz = sm.red[0];
+    row_sync<W>();
+}
+
+
+template <int W, int ITEMS, bool SV>
+__device__ void numeric_row(const Job& J, int row, RowSmem<W, ITEMS, SV>& sm, double* vals, ErrWord* err) {
+    using Sm = RowSmem<W, ITEMS, SV>;
+    constexpr int kSeqBits = Sm::kSeqBits;
+    const int lane = threadIdx.x & 31;
+    const int warp = W == 1 ? 0 : (threadIdx.x >> 5);
+    const int tid = W == 1 ? lane : threadIdx.x;
+    const int P = static_cast<int>(J.ub[row]);
+    if (W > 1 && tid == 0) sm.kept = 0;  // read only after the barriers below
+
+    // 1. products into shared memory
+    int32_t lo = INT32_MAX, hi = INT32_MIN;
+    const int32_t ncols = J.B.cols;
+    team_products<W * 32, true, int32_t>(J, row, sm.seg, sm.warp_tmp, tid, [&](int32_t seq, int32_t c, double b, double a) {
+        if (c < 0 || c >= ncols) {
+            raise_error(err, kErrInvalid, 4, c);
+            c = 0;
+        }
+        sm.keys[seq] = static_cast<uint32_t>(c);
+        vals[seq] = __dmul_rn(a, b);
+        lo = min(lo, c);
+        hi = max(hi, c);
+    });
+    lo = warp_min(lo);
+    hi = warp_max(hi);
+    if (W > 1) {
+        if (lane == 0) {
+            sm.red[warp] = lo;
+            sm.red[W + warp] = hi;
+        }
+        __syncthreads();
+        lo = sm.red[0];
+        hi = sm.red[W];
+#pragma unroll
+        for (int w = 1; w < W; ++w) {
+            lo = min(lo, sm.red[w]);
+            hi = max(hi, sm.red[W + w]);
+        }
+    }
+    row_sync<W>();
+    const uint32_t cmin = static_cast<uint32_t>(lo);
+    const uint32_t range = P ? static_cast<uint32_t>(hi - lo) : 0u;
+    const int nbits = range ? 32 - __clz(range) : 0;
+    const RowOut out{J.c_col, J.c_val, J.cnt[row], J.nz + row, J.holes};
+    if (nbits + kSeqBits <= 32) finish_row<W, ITEMS, SV, true>(out, sm, vals, P, cmin, nbits, lane, warp, tid);
+    else finish_row<W, ITEMS, SV, false>(out, sm, vals, P, cmin, nbits, lane, warp, tid);
+}
+
+constexpr int kWarpKernelThreads = 256;
+
+template <int ITEMS>
+__global__ void __launch_bounds__(kWarpKernelThreads)
+num_warp_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items, int64_t count,
+                Stats* __restrict__ stats, ErrWord* __restrict__ err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    using Sm = RowSmem<1, ITEMS>;
+    Sm& sm = reinterpret_cast<Sm*>(smem_raw)[threadIdx.x >> 5];
+    __shared__ unsigned long long s_nz;
+    if (threadIdx.x == 0) s_nz = 0;
+    __syncthreads();
+    const int64_t warps = static_cast<int64_t>(gridDim.x) * (kWarpKernelThreads / 32);
+    unsigned long long mine = 0;
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * (kWarpKernelThreads / 32) + (threadIdx.x >> 5); i < count;
+         i += warps) {
+        const int64_t it = items[i];
+        const Job& J = jobs[item_job(it)];
+        const int row = item_row(it);
+        numeric_row<1, ITEMS, true>(J, row, sm, sm.vals, err);
+        if ((threadIdx.x & 31) == 0) mine += static_cast<unsigned long long>(J.nz[row]);
+    }
+    if ((threadIdx.x & 31) == 0 && mine) atomicAdd(&s_nz, mine);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_nz) atomicAdd(&stats->nz_total, s_nz);
+}
+
+template <int W, int ITEMS, int MINB, bool SV>
+__global__ void __launch_bounds__(W * 32, MINB)
+num_block_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items, int64_t count,
+                 Stats* __restrict__ stats, ErrWord* __restrict__ err, double* __restrict__ gvals) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    using Sm = RowSmem<W, ITEMS, SV>;
+    Sm& sm = *reinterpret_cast<Sm*>(smem_raw);
+    double* vals = SV ? sm.vals : gvals + static_cast<size_t>(blockIdx.x) * Sm::kCap;
+    unsigned long long mine = 0;
+    for (int64_t i = blockIdx.x; i < count; i += gridDim.x) {
+        const int64_t it = items[i];
+        const Job& J = jobs[item_job(it)];
+        const int row = item_row(it);
+        numeric_row<W, ITEMS, SV>(J, row, sm, vals, err);
+        if (threadIdx.x == 0) mine += static_cast<unsigned long long>(J.nz[row]);
+    }
+    if (threadIdx.x == 0 && mine) atomicAdd(&stats->nz_total, mine);
+}
+
+inline int capped(int64_t work, int per_block, int cap) {
+    const int64_t g = (work + per_block - 1) / per_block;
+    return static_cast<int>(g < 1 ? 1 : (g > cap ? cap : g));
+}
+
+// CTAs of a launch whose CTAs each own a global slab: one per SM at most.
+inline int slab_grid(int64_t count, int num_sms) { return static_cast<int>(count < num_sms ? count : num_sms); }
+
+template <int ITEMS>
+void run_warp(const Job* jobs, const int64_t* items, int64_t count, Stats* stats, ErrWord* err, cudaStream_t st,
+              int num_sms) {
+    const int smem = 8 * static_cast<int>(sizeof(RowSmem<1, ITEMS>));
+    cudaFuncSetAttribute(num_warp_kernel<ITEMS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    num_warp_kernel<ITEMS><<<capped(count, 8, num_sms * 16), kWarpKernelThreads, smem, st>>>(jobs, items, count, stats,
+                                                                                           err);
+}
+
+template <int W, int ITEMS, int MINB, bool SV = true>
+void run_block(const Job* jobs, const int64_t* items, int64_t count, Stats* stats, ErrWord* err, cudaStream_t st,
+               int num_sms, double* gvals = nullptr) {
+    const int smem = static_cast<int>(sizeof(RowSmem<W, ITEMS, SV>));
+    cudaFuncSetAttribute(num_block_kernel<W, ITEMS, MINB, SV>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    const int grid = SV ? capped(count, 1, num_sms * 8) : slab_grid(count, num_sms);
+    num_block_kernel<W, ITEMS, MINB, SV><<<grid, W * 32, smem, st>>>(jobs, items, count, stats, err, gvals);
+}
+
+}  // namespace
+}  // namespace spg

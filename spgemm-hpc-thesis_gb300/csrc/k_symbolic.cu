@@ -154,7 +154,8 @@ int heavy_ctas(int64_t count, int num_sms) { return static_cast<int>(count < num
 }  // namespace
 
 size_t symbolic_scratch_bytes(const int64_t* bin_count, int64_t max_ub, int num_sms) {
-    const int64_t count = std::max(bin_count[kBinB16K], bin_count[kBinHeavy]);
+    int64_t count = 0;  // the global-hash bins run one after the other
+    for (int b = kLastSmemBin + 1; b < kNumBins; ++b) count = std::max(count, bin_count[b]);
     if (count == 0) return 0;
     return static_cast<size_t>(heavy_ctas(count, num_sms)) * (size_t{1} << ceil_log2(2 * max_ub)) * sizeof(int32_t);
 }
@@ -162,10 +163,10 @@ size_t symbolic_scratch_bytes(const int64_t* bin_count, int64_t max_ub, int num_
 void launch_symbolic(int bin, const Job* d_jobs, const int64_t* d_items, int64_t count, int64_t max_ub,
                      void* d_scratch, size_t, Stats*, ErrWord* d_err, cudaStream_t stream, int num_sms) {
     if (count <= 0) return;
-    if (bin <= kBinW16) {
+    if (bin <= kLastWarpBin) {
         const int grid = capped_grid(count, kSymWarpThreads / 32, num_sms * 32);
-        sym_warp_kernel<<<grid, kSymWarpThreads, 0, stream>>>(d_jobs, d_items, count, bin == kBinW1, d_err);
-    } else if (bin <= kBinB8K) {
+        sym_warp_kernel<<<grid, kSymWarpThreads, 0, stream>>>(d_jobs, d_items, count, bin == 1, d_err);
+    } else if (bin <= kLastSmemBin) {
         const int smem = kSymBlockTable * sizeof(int32_t);
         cudaFuncSetAttribute(sym_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         const int grid = capped_grid(count, 1, num_sms * 8);

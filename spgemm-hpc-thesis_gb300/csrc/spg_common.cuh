@@ -41,22 +41,20 @@ struct Job {
                               // column -1 marking unused slots (upper-bound mode); 0: compacted
 };
 
-// Row bins by product count (ub).  Bin b covers (kBinHi[b-1], kBinHi[b]].
-enum Bin : int {
-    kBinEmpty = 0,
-    kBinW1,    // <= 32       warp, 1 item per lane
-    kBinW2,    // <= 64       warp, 2 items
-    kBinW4,    // <= 128
-    kBinW8,    // <= 256
-    kBinW16,   // <= 512
-    kBinB1K,   // <= 1024     4 warps x 8 items
-    kBinB2K,   // <= 2048     8 warps x 8 items
-    kBinB4K,   // <= 4096     8 warps x 16 items
-    kBinB8K,   // <= 8192     16 warps x 16 items
-    kBinB16K,  // <= 16384    16 warps x 32 items, product values in a global slab
-    kBinHeavy, // >  16384    one CTA per row, sort in global memory
-    kNumBins
-};
+// Row bins by product count (ub): capacities 32, 64, then two per power of two
+// (3/4 of it and all of it) up to 16384, so that a row fills on average ~85%
+// of its bin's slots.  Bin b covers (capacity(b-1), capacity(b)].
+//   bins 1-8   warp per row (1, 2, 3, 4, 6, 8, 12, 16 items per lane):
+//              <= 32, 64, 96, 128, 192, 256, 384, 512 products
+//   bins 9-16  CTA per row, everything in shared memory:
+//              <= 768, 1024, 1536, 2048, 3072, 4096, 6144, 8192
+//   bins 17-18 CTA per row, product values in a global slab: <= 12288, 16384
+//   bin 19     heavier rows: CTA per row, sort in global memory
+constexpr int kBinEmpty = 0;
+constexpr int kLastWarpBin = 8;     // capacity 512
+constexpr int kLastSmemBin = 16;    // capacity 8192
+constexpr int kBinHeavy = 19;
+constexpr int kNumBins = 20;
 constexpr int64_t kHeavyThreshold = 16384;
 
 __host__ __device__ inline int clz64(unsigned long long x) {
@@ -67,17 +65,23 @@ __host__ __device__ inline int clz64(unsigned long long x) {
 #endif
 }
 
-// 0 for ub == 0, kBinHeavy above kHeavyThreshold, else max(1, ceil(log2 ub) - 4).
+// Bin of a row with ub scalar products (0 for ub == 0).
 __host__ __device__ inline int bin_of(int64_t ub) {
     if (ub <= 0) return kBinEmpty;
     if (ub > kHeavyThreshold) return kBinHeavy;
-    if (ub <= 32) return kBinW1;
-    return (64 - clz64(static_cast<unsigned long long>(ub - 1))) - 4;
+    if (ub <= 32) return 1;
+    if (ub <= 64) return 2;
+    const int b = 64 - clz64(static_cast<unsigned long long>(ub - 1));  // ceil(log2 ub), 7..14
+    return 2 * (b - 7) + 3 + (ub > (int64_t{3} << (b - 2)) ? 1 : 0);
 }
 
 // Largest product count of a bin (its capacity).
 __host__ __device__ inline int64_t bin_capacity(int b) {
-    return b == kBinEmpty ? 0 : (b == kBinHeavy ? INT64_MAX : (int64_t{16} << b));
+    if (b == kBinEmpty) return 0;
+    if (b == kBinHeavy) return INT64_MAX;
+    if (b <= 2) return int64_t{32} << (b - 1);
+    const int e = (b - 3) / 2 + 7;  // power of two of the bin pair
+    return (b - 3) % 2 == 0 ? (int64_t{3} << (e - 2)) : (int64_t{1} << e);
 }
 
 // Error word written by kernels (first error wins) and read by the host at
@@ -186,6 +190,9 @@ size_t scan_partials_count(int64_t n);
 void launch_numeric(int bin, const Job* d_jobs, const int64_t* d_items, int64_t count, int64_t max_ub,
                     void* d_scratch, size_t scratch_bytes, Stats* d_stats, ErrWord* d_err,
                     cudaStream_t stream, int num_sms);
+// K4 for the warp-per-row bins (1..kLastWarpBin), compiled separately.
+void launch_numeric_warp(int bin, const Job* d_jobs, const int64_t* d_items, int64_t count, Stats* d_stats,
+                         ErrWord* d_err, cudaStream_t stream, int num_sms);
 // Global scratch of the numeric phase (value slabs of the 16K bin, sort slabs
 // of heavy rows; the two launches run one after the other and share it).
 size_t numeric_scratch_bytes(const int64_t* bin_count, int64_t max_ub, int num_sms);

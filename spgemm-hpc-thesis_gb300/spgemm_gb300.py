@@ -27,8 +27,8 @@ SPG_HOST, SPG_DEVICE = 0, 1
 STATUS_NAMES = {0: "SPG_OK", 1: "SPG_INVALID_ARGUMENT", 2: "SPG_OVERFLOW", 3: "SPG_OUT_OF_RANGE_COLUMN",
                 4: "SPG_OUT_OF_MEMORY", 5: "SPG_BUDGET_EXCEEDED", 6: "SPG_DEVICE_TIMEOUT", 7: "SPG_CUDA_ERROR",
                 8: "SPG_NOT_READY", 9: "SPG_CANCELLED"}
-BIN_NAMES = ["empty", "w<=32", "w<=64", "w<=128", "w<=256", "w<=512", "b<=1K", "b<=2K", "b<=4K", "b<=8K", "b<=16K",
-             "heavy"]
+BIN_NAMES = ["empty", "w<=32", "w<=64", "w<=96", "w<=128", "w<=192", "w<=256", "w<=384", "w<=512", "b<=768",
+             "b<=1K", "b<=1.5K", "b<=2K", "b<=3K", "b<=4K", "b<=6K", "b<=8K", "b<=12K", "b<=16K", "heavy"]
 
 
 @dataclass
@@ -100,8 +100,8 @@ MODES = {"auto": 0, "exact": 1, "upper_bound": 2}
 class Timings(C.Structure):
     _fields_ = [("ms_rowwork", C.c_float), ("ms_symbolic", C.c_float), ("ms_scan", C.c_float),
                 ("ms_numeric", C.c_float), ("ms_compact", C.c_float), ("ms_total", C.c_float),
-                ("products", C.c_int64), ("nnz", C.c_int64), ("rows", C.c_int64), ("bin_rows", C.c_int64 * 12),
-                ("launches", C.c_int64), ("ms_numeric_bin", C.c_float * 12)]
+                ("products", C.c_int64), ("nnz", C.c_int64), ("rows", C.c_int64), ("bin_rows", C.c_int64 * 20),
+                ("launches", C.c_int64), ("ms_numeric_bin", C.c_float * 20)]
 
     def as_dict(self) -> dict:
         d = {k: getattr(self, k) for k, _ in self._fields_ if k not in ("bin_rows", "ms_numeric_bin")}

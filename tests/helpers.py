@@ -75,8 +75,9 @@ def row_sizes_for_bins(seed: int):
     """(A, B) whose rows cover every product-count bin of the engine, the
     heavy (> 16384 products) one included."""
     rng = np.random.default_rng(seed)
-    targets = [0, 1, 7, 32, 33, 64, 65, 100, 128, 129, 256, 257, 400, 512, 513, 900, 1024, 1025, 2000, 2048, 2049,
-               3000, 4096, 4097, 6000, 8192, 8193, 12000, 16384, 16385, 30000]
+    targets = [0, 1, 7, 32, 33, 64, 65, 96, 97, 128, 129, 192, 193, 256, 257, 384, 385, 512, 513, 768, 769, 1024,
+               1025, 1536, 1537, 2048, 2049, 3072, 3073, 4096, 4097, 6144, 6145, 8192, 8193, 12288, 12289, 16384,
+               16385, 30000]
     lens = rng.integers(0, 41, size=4000)
     lens[:100] = 1  # rows of one entry make every exact product count reachable
     b = random_csr(4000, 3000, lens, seed + 1)

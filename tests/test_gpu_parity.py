@@ -49,8 +49,8 @@ def test_every_bin(engine, port, seed):
     a, b = row_sizes_for_bins(seed)
     check(engine, port, a, b)
     t = engine.last_timings()
-    assert t["bin_rows"]["heavy"] >= 2 and t["bin_rows"]["b<=16K"] >= 3 and t["bin_rows"]["b<=8K"] >= 1
-    assert t["bin_rows"]["w<=32"] >= 1
+    from spgemm_gb300 import BIN_NAMES
+    assert all(t["bin_rows"][name] >= 1 for name in BIN_NAMES), t["bin_rows"]
 
 
 def test_known_answer(engine):
