@@ -299,7 +299,7 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
     // of its product count (ub) and compacted afterwards; in the exact mode a
     // symbolic phase counts the distinct columns of every row first.
     const bool exact = use_exact_mode(h, products, ar.bytes());
-    size_t scratch_bytes = numeric_scratch_bytes(bin_count, max_ub, h->num_sms);
+    size_t scratch_bytes = numeric_scratch_bytes(bin_count, max_ub, h->num_sms, !exact);
     if (exact) scratch_bytes = std::max(scratch_bytes, symbolic_scratch_bytes(bin_count, max_ub, h->num_sms));
     void* scratch = scratch_bytes ? ar.alloc<unsigned char>(scratch_bytes, "heavy scratch") : nullptr;
     int64_t* partials = ar.alloc<int64_t>(scan_partials_count(static_cast<int64_t>(slots)), "scan partials");
@@ -341,7 +341,7 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
     for (int b = 1; b < kNumBins; ++b) {
         if (!bin_count[b]) continue;
         launch_numeric(b, d_jobs, items + bin_off[b], bin_count[b], max_ub, scratch, scratch_bytes, &d_ctrl->stats,
-                       &d_ctrl->err, st, h->num_sms);
+                       &d_ctrl->err, st, h->num_sms, !exact);
         cudaEventRecord(h->bin_ev[b], st);
     }
     check_cuda(cudaGetLastError(), "K4 launch");

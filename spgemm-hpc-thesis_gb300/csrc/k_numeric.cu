@@ -46,7 +46,9 @@ __device__ inline HeavySlab heavy_slab(void* base, int64_t cap, int cta) {
 
 __global__ void __launch_bounds__(kHeavyThreads)
 num_heavy_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items, int64_t count, void* slabs,
-                 int64_t cap, Stats* __restrict__ stats, ErrWord* __restrict__ err) {
+                 int64_t cap, Stats* __restrict__ stats, ErrWord* __restrict__ err,
+                 const unsigned long long* __restrict__ d_count) {
+    if (d_count) count = static_cast<int64_t>(*d_count);  // rows left over by the piece planner
     __shared__ HeavySmem sm;
     const HeavySlab sl = heavy_slab(slabs, cap, blockIdx.x);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, tid = threadIdx.x;
@@ -217,6 +219,159 @@ num_heavy_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items
     if (tid == 0 && kept_total) atomicAdd(&stats->nz_total, kept_total);
 }
 
+// ---------------------------------------------------------------------------
+// Heavy rows in upper-bound mode: split by column range into pieces of at
+// most kPieceCap products, which run on the CTA pipeline of the 16384-product
+// bin (keys in shared memory, values in a global slab), many pieces of one row
+// in parallel.  The planner histograms the row's product columns into
+// kPlanBuckets buckets of the column space and cuts greedily: each piece takes
+// the longest run of buckets that still fits kPieceCap (a binary search over
+// the bucket prefixes).  Rows with a bucket above kPieceCap or more than
+// kMaxPieces pieces keep the global-slab path.  A piece owns the slots of its
+// products in the row's reserved range (the products of earlier pieces have
+// smaller columns, so they sort first).
+constexpr int kPlanThreads = 512;
+constexpr int kPlanBuckets = 4096;
+constexpr uint32_t kPieceCap = 16383;
+constexpr int kMaxPieces = 256;
+constexpr int kPieceW = 16, kPieceItems = 32;
+
+struct HeavyPlan {
+    unsigned long long* counters;  // [0] pieces, [1] rows left to the global-slab path
+    Piece* pieces;
+    int64_t* fallback;
+    int64_t max_pieces;
+};
+
+struct PlanSmem {
+    SegTab<kPlanThreads, int32_t> seg;
+    int64_t warp_tmp[kPlanThreads / 32 + 1];
+    uint32_t bucket[kPlanBuckets];  // counts, then exclusive prefixes
+    int32_t start[kMaxPieces + 1];
+    uint32_t maxc;
+    int32_t npieces;
+    unsigned long long base;
+};
+
+__global__ void __launch_bounds__(kPlanThreads)
+heavy_plan_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items, int64_t count, HeavyPlan plan,
+                  ErrWord* __restrict__ err) {
+    __shared__ PlanSmem sm;
+    constexpr int kPer = kPlanBuckets / kPlanThreads;
+    const int tid = threadIdx.x, lane = tid & 31;
+    for (int64_t i = blockIdx.x; i < count; i += gridDim.x) {
+        const int64_t it = items[i];
+        const Job& J = jobs[item_job(it)];
+        const int row = item_row(it);
+        const int32_t ncols = J.B.cols;
+        const int shift = max(0, ceil_log2(max(ncols, 1)) - 12);  // 4096 << shift >= ncols
+        for (int k = tid; k < kPlanBuckets; k += kPlanThreads) sm.bucket[k] = 0;
+        if (tid == 0) sm.maxc = 0;
+        __syncthreads();
+        team_products<kPlanThreads, false, int32_t>(J, row, sm.seg, sm.warp_tmp, tid,
+                                                    [&](int32_t, int32_t c, double, double) {
+                                                        if (c < 0 || c >= ncols) c = 0;
+                                                        atomicAdd(&sm.bucket[c >> shift], 1u);
+                                                    });
+        uint32_t v[kPer];
+        uint32_t sum = 0, mx = 0;
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            v[j] = sm.bucket[tid * kPer + j];
+            sum += v[j];
+            mx = max(mx, v[j]);
+        }
+        mx = warp_max(mx);
+        if (lane == 0) atomicMax(&sm.maxc, mx);
+        uint32_t run = block_incl_scan<kPlanThreads>(sum, sm.warp_tmp) - sum;
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            sm.bucket[tid * kPer + j] = run;
+            run += v[j];
+        }
+        __syncthreads();
+        const uint32_t total = static_cast<uint32_t>(J.ub[row]);
+        if (tid == 0) {
+            // greedy cut: prefix(e) = sm.bucket[e] (exclusive) for e < kPlanBuckets, total at the end
+            auto prefix = [&](int e) { return e < kPlanBuckets ? sm.bucket[e] : total; };
+            int np = 0, k = 0;
+            bool ok = sm.maxc <= kPieceCap;
+            while (ok && k < kPlanBuckets) {
+                if (np == kMaxPieces) {
+                    ok = false;
+                    break;
+                }
+                sm.start[np++] = k;
+                int lo = k + 1, hi = kPlanBuckets;  // largest e in [lo, hi] with prefix(e) - prefix(k) <= cap
+                const uint32_t limit = prefix(k) + kPieceCap;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (prefix(mid) <= limit) lo = mid;
+                    else hi = mid - 1;
+                }
+                k = lo;
+            }
+            sm.npieces = ok ? np : 0;
+            if (ok) {
+                sm.start[np] = kPlanBuckets;
+                sm.base = atomicAdd(plan.counters, static_cast<unsigned long long>(np));
+                if (sm.base + np > static_cast<unsigned long long>(plan.max_pieces))
+                    raise_error(err, kErrOverflow, 7, static_cast<int64_t>(sm.base + np));
+            } else {
+                plan.fallback[atomicAdd(plan.counters + 1, 1ull)] = it;
+            }
+        }
+        __syncthreads();
+        if (tid < sm.npieces && sm.base + tid < static_cast<unsigned long long>(plan.max_pieces)) {
+            const int k0 = sm.start[tid], k1 = sm.start[tid + 1];
+            Piece pc;
+            pc.item = it;
+            pc.lo = k0 << shift;
+            pc.hi = k1 < kPlanBuckets ? (k1 << shift) : INT32_MAX;
+            pc.slot_off = sm.bucket[k0];
+            pc.count = static_cast<int64_t>(k1 < kPlanBuckets ? sm.bucket[k1] : total) - pc.slot_off;
+            plan.pieces[sm.base + tid] = pc;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(kPieceW * 32, 1)
+num_piece_kernel(const Job* __restrict__ jobs, HeavyPlan plan, Stats* __restrict__ stats, ErrWord* __restrict__ err,
+                 double* __restrict__ gvals) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    using Sm = RowSmem<kPieceW, kPieceItems, false>;
+    Sm& sm = *reinterpret_cast<Sm*>(smem_raw);
+    double* vals = gvals + static_cast<size_t>(blockIdx.x) * Sm::kCap;
+    const int64_t count = min(static_cast<int64_t>(*plan.counters), plan.max_pieces);
+    unsigned long long mine = 0;
+    for (int64_t i = blockIdx.x; i < count; i += gridDim.x) {
+        const Piece pc = plan.pieces[i];
+        if (pc.count <= 0) continue;  // an empty last piece (same for the whole CTA)
+        const Job& J = jobs[item_job(pc.item)];
+        numeric_row<kPieceW, kPieceItems, false, true>(J, item_row(pc.item), sm, vals, err, &pc);
+        if (threadIdx.x == 0) mine += sm.kept;
+    }
+    if (threadIdx.x == 0 && mine) atomicAdd(&stats->nz_total, mine);
+}
+
+// Scratch layout of the heavy bin in upper-bound mode.
+struct HeavyLayout {
+    size_t pieces_off, fallback_off, slab_off, bytes;
+    int64_t max_pieces;
+};
+
+HeavyLayout heavy_layout(int64_t count, int64_t max_ub, size_t slab_bytes) {
+    HeavyLayout L;
+    L.max_pieces = count * (2 * (max_ub / kPieceCap) + 4);  // two neighbouring greedy pieces exceed the cap
+    auto up = [](size_t x) { return (x + 255) & ~size_t{255}; };
+    L.pieces_off = 256;
+    L.fallback_off = up(L.pieces_off + static_cast<size_t>(L.max_pieces) * sizeof(Piece));
+    L.slab_off = up(L.fallback_off + static_cast<size_t>(count) * sizeof(int64_t));
+    L.bytes = L.slab_off + slab_bytes;
+    return L;
+}
+
 int heavy_grid(int64_t count, int num_sms) { return static_cast<int>(count < num_sms ? count : num_sms); }
 
 // Product-value slab of one CTA of the two global-slab bins.
@@ -224,19 +379,27 @@ constexpr int64_t slab_cap(int bin) { return bin == 17 ? 16 * 32 * 24 : 16 * 32 
 
 }  // namespace
 
-size_t numeric_scratch_bytes(const int64_t* bin_count, int64_t max_ub, int num_sms) {
+size_t numeric_scratch_bytes(const int64_t* bin_count, int64_t max_ub, int num_sms, bool holes) {
     size_t need = 0;
     for (int b = kLastSmemBin + 1; b < kBinHeavy; ++b)  // the launches run one after the other
         if (bin_count[b])
             need = std::max(need, static_cast<size_t>(slab_grid(bin_count[b], num_sms)) * slab_cap(b) * sizeof(double));
-    if (bin_count[kBinHeavy])
-        need = std::max(need, static_cast<size_t>(heavy_grid(bin_count[kBinHeavy], num_sms)) * 24 *
-                                  static_cast<size_t>(max_ub));
+    const int64_t heavy = bin_count[kBinHeavy];
+    if (heavy) {
+        const size_t global_slab = static_cast<size_t>(heavy_grid(heavy, num_sms)) * 24 * static_cast<size_t>(max_ub);
+        if (holes) {
+            const size_t piece_slab = static_cast<size_t>(num_sms) * kPieceW * 32 * kPieceItems * sizeof(double);
+            need = std::max(need, heavy_layout(heavy, max_ub, std::max(global_slab, piece_slab)).bytes);
+        } else {
+            need = std::max(need, global_slab);
+        }
+    }
     return need;
 }
 
 void launch_numeric(int bin, const Job* d_jobs, const int64_t* d_items, int64_t count, int64_t max_ub,
-                    void* d_scratch, size_t, Stats* d_stats, ErrWord* d_err, cudaStream_t st, int num_sms) {
+                    void* d_scratch, size_t, Stats* d_stats, ErrWord* d_err, cudaStream_t st, int num_sms,
+                    bool holes) {
     if (count <= 0) return;
     if (bin <= kLastWarpBin) {
         launch_numeric_warp(bin, d_jobs, d_items, count, d_stats, d_err, st, num_sms);
@@ -255,8 +418,31 @@ void launch_numeric(int bin, const Job* d_jobs, const int64_t* d_items, int64_t 
         case 17: run_block<16, 24, 1, false>(d_jobs, d_items, count, d_stats, d_err, st, num_sms, slab); break;
         case 18: run_block<16, 32, 1, false>(d_jobs, d_items, count, d_stats, d_err, st, num_sms, slab); break;
         case kBinHeavy:
-            num_heavy_kernel<<<heavy_grid(count, num_sms), kHeavyThreads, 0, st>>>(d_jobs, d_items, count, d_scratch,
-                                                                                   max_ub, d_stats, d_err);
+            if (holes) {
+                const size_t global_slab = static_cast<size_t>(heavy_grid(count, num_sms)) * 24 * static_cast<size_t>(max_ub);
+                const size_t piece_slab = static_cast<size_t>(num_sms) * kPieceW * 32 * kPieceItems * sizeof(double);
+                const HeavyLayout L = heavy_layout(count, max_ub, std::max(global_slab, piece_slab));
+                unsigned char* base = static_cast<unsigned char*>(d_scratch);
+                HeavyPlan plan;
+                plan.counters = reinterpret_cast<unsigned long long*>(base);
+                plan.pieces = reinterpret_cast<Piece*>(base + L.pieces_off);
+                plan.fallback = reinterpret_cast<int64_t*>(base + L.fallback_off);
+                plan.max_pieces = L.max_pieces;
+                void* slabs = base + L.slab_off;
+                cudaMemsetAsync(plan.counters, 0, 2 * sizeof(unsigned long long), st);
+                heavy_plan_kernel<<<static_cast<int>(std::min<int64_t>(count, 2 * num_sms)), kPlanThreads, 0, st>>>(
+                    d_jobs, d_items, count, plan, d_err);
+                using PieceSm = RowSmem<kPieceW, kPieceItems, false>;
+                const int smem = static_cast<int>(sizeof(PieceSm));
+                cudaFuncSetAttribute(num_piece_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+                num_piece_kernel<<<num_sms, kPieceW * 32, smem, st>>>(d_jobs, plan, d_stats, d_err,
+                                                                      static_cast<double*>(slabs));
+                num_heavy_kernel<<<heavy_grid(count, num_sms), kHeavyThreads, 0, st>>>(
+                    d_jobs, plan.fallback, count, slabs, max_ub, d_stats, d_err, plan.counters + 1);
+            } else {
+                num_heavy_kernel<<<heavy_grid(count, num_sms), kHeavyThreads, 0, st>>>(
+                    d_jobs, d_items, count, d_scratch, max_ub, d_stats, d_err, nullptr);
+            }
             break;
         default: break;
     }

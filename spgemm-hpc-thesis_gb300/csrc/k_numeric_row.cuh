@@ -64,6 +64,7 @@ struct RowSmem {
     uint16_t seqs[kCap];        // sequence numbers of the unpacked path
     int32_t red[2 * W];         // min / max column reduction
     uint32_t kept;              // stored entries of the row (upper-bound mode)
+    uint32_t step_cnt[64];      // kept counts of one filtered enumeration step (row pieces)
 };
 
 // Exclusive scan of the 256*W digit counters in (digit, warp) order, 8
@@ -160,6 +161,7 @@ struct RowOut {
     int64_t out0;       // first slot of the row in C_tmp
     int64_t* nz;        // the row's stored-entry count
     int32_t holes;      // upper-bound mode: slot-per-position output with holes
+    int32_t nz_add;     // a piece of a split row: add to *nz instead of storing it
 };
 
 // Steps 2-4 of a row for one key layout (PACKED: (col - cmin) << kSeqBits | seq
@@ -304,7 +306,10 @@ __device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double*
         } else {
             if (lane == 0) atomicAdd(&sm.kept, kept);
             __syncthreads();
-            if (tid == 0) *out.nz = sm.kept;
+            if (tid == 0) {
+                if (out.nz_add) atomicAdd(reinterpret_cast<unsigned long long*>(out.nz), sm.kept);
+                else *out.nz = sm.kept;
+            }
         }
         row_sync<W>();
         return;
@@ -360,20 +365,36 @@ __device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double*
 }
 
 
-template <int W, int ITEMS, bool SV>
-__device__ void numeric_row(const Job& J, int row, RowSmem<W, ITEMS, SV>& sm, double* vals, ErrWord* err) {
+// A column range of a split row: the products with columns in [lo, hi), which
+// own slots [slot_off, slot_off + count) of the row's reserved range.
+struct Piece {
+    int64_t item;
+    int32_t lo, hi;
+    int64_t slot_off;
+    int64_t count;
+};
+
+// One row (PIECE = false) or one column range of a row (PIECE = true, CTA
+// rows in upper-bound mode only).
+template <int W, int ITEMS, bool SV, bool PIECE = false>
+__device__ void numeric_row(const Job& J, int row, RowSmem<W, ITEMS, SV>& sm, double* vals, ErrWord* err,
+                            const Piece* pc = nullptr) {
     using Sm = RowSmem<W, ITEMS, SV>;
     constexpr int kSeqBits = Sm::kSeqBits;
     const int lane = threadIdx.x & 31;
     const int warp = W == 1 ? 0 : (threadIdx.x >> 5);
     const int tid = W == 1 ? lane : threadIdx.x;
-    const int P = static_cast<int>(J.ub[row]);
+    const int P = static_cast<int>(PIECE ? pc->count : J.ub[row]);
     if (W > 1 && tid == 0) sm.kept = 0;  // read only after the barriers below
 
     // 1. products into shared memory
     int32_t lo = INT32_MAX, hi = INT32_MIN;
     const int32_t ncols = J.B.cols;
-    team_products<W * 32, true, int32_t>(J, row, sm.seg, sm.warp_tmp, tid, [&](int32_t seq, int32_t c, double b, double a) {
+    auto take = [&](int32_t seq, int32_t c, double b, double a) {
+        if (PIECE && seq >= P) {  // the planner counted fewer products in this range: never writes past P
+            raise_error(err, kErrInvalid, 8, seq);
+            return;
+        }
         if (c < 0 || c >= ncols) {
             raise_error(err, kErrInvalid, 4, c);
             c = 0;
@@ -382,7 +403,11 @@ __device__ void numeric_row(const Job& J, int row, RowSmem<W, ITEMS, SV>& sm, do
         vals[seq] = __dmul_rn(a, b);
         lo = min(lo, c);
         hi = max(hi, c);
-    });
+    };
+    if constexpr (PIECE)
+        team_products_in<W * 32>(J, row, sm.seg, sm.warp_tmp, sm.step_cnt, tid, pc->lo, pc->hi, take);
+    else
+        team_products<W * 32, true, int32_t>(J, row, sm.seg, sm.warp_tmp, tid, take);
     lo = warp_min(lo);
     hi = warp_max(hi);
     if (W > 1) {
@@ -403,7 +428,7 @@ __device__ void numeric_row(const Job& J, int row, RowSmem<W, ITEMS, SV>& sm, do
     const uint32_t cmin = static_cast<uint32_t>(lo);
     const uint32_t range = P ? static_cast<uint32_t>(hi - lo) : 0u;
     const int nbits = range ? 32 - __clz(range) : 0;
-    const RowOut out{J.c_col, J.c_val, J.cnt[row], J.nz + row, J.holes};
+    const RowOut out{J.c_col, J.c_val, J.cnt[row] + (PIECE ? pc->slot_off : 0), J.nz + row, J.holes, PIECE ? 1 : 0};
     if (nbits + kSeqBits <= 32) finish_row<W, ITEMS, SV, true>(out, sm, vals, P, cmin, nbits, lane, warp, tid);
     else finish_row<W, ITEMS, SV, false>(out, sm, vals, P, cmin, nbits, lane, warp, tid);
 }

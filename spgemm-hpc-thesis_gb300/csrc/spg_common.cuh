@@ -187,15 +187,17 @@ size_t symbolic_scratch_bytes(const int64_t* bin_count, int64_t max_ub, int num_
 void launch_scan(int64_t* d_data, int64_t n, int64_t* d_partials, cudaStream_t stream);
 size_t scan_partials_count(int64_t n);
 // K4: sorted, summed, zero-free rows into job.c_col/c_val and job.nz[row].
+// holes: upper-bound layout (rows above 16384 products are then split into
+// column-range pieces; in the exact layout they keep the global-slab sort).
 void launch_numeric(int bin, const Job* d_jobs, const int64_t* d_items, int64_t count, int64_t max_ub,
                     void* d_scratch, size_t scratch_bytes, Stats* d_stats, ErrWord* d_err,
-                    cudaStream_t stream, int num_sms);
+                    cudaStream_t stream, int num_sms, bool holes);
 // K4 for the warp-per-row bins (1..kLastWarpBin), compiled separately.
 void launch_numeric_warp(int bin, const Job* d_jobs, const int64_t* d_items, int64_t count, Stats* d_stats,
                          ErrWord* d_err, cudaStream_t stream, int num_sms);
 // Global scratch of the numeric phase (value slabs of the 16K bin, sort slabs
 // of heavy rows; the two launches run one after the other and share it).
-size_t numeric_scratch_bytes(const int64_t* bin_count, int64_t max_ub, int num_sms);
+size_t numeric_scratch_bytes(const int64_t* bin_count, int64_t max_ub, int num_sms, bool holes);
 // K5: move rows from C_tmp (offsets job.cnt) to C (offsets job.nz, scanned).
 void launch_compact(const Job* d_job, int rows, int32_t* out_col, double* out_val, cudaStream_t stream);
 // K5 for rows written with holes: keeps the slots whose column is >= 0.
