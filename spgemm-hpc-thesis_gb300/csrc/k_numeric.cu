@@ -407,11 +407,11 @@ void launch_numeric(int bin, const Job* d_jobs, const int64_t* d_items, int64_t 
     }
     double* slab = static_cast<double*>(d_scratch);
     switch (bin) {
-        case 9: run_block<4, 6, 6>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;     // <= 768
+        case 9: run_block<3, 8, 8>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;     // <= 768
         case 10: run_block<4, 8, 6>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;    // <= 1024
-        case 11: run_block<8, 6, 3>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;    // <= 1536
+        case 11: run_block<6, 8, 4>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;    // <= 1536
         case 12: run_block<8, 8, 3>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;    // <= 2048
-        case 13: run_block<8, 12, 2>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;   // <= 3072
+        case 13: run_block<12, 8, 2>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;   // <= 3072
         case 14: run_block<8, 16, 2>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;   // <= 4096
         case 15: run_block<16, 12, 1>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;  // <= 6144
         case 16: run_block<16, 16, 1>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;  // <= 8192

@@ -38,14 +38,16 @@ __device__ inline void row_sync() {
 constexpr int log2_ceil_c(int x) { return x <= 1 ? 0 : 1 + log2_ceil_c((x + 1) / 2); }
 
 // Digit counters of W warps: counter (digit d, warp w) lives at hidx<W>(d, w),
-// digit-major with one padding word after every W counters.  (W + 1) is odd, so
-// the counters that one warp's lanes touch for different digits fall in
-// different banks; without the padding they would share 32 / W banks.
+// digit-major with an odd stride kHistStride >= W, so that the counters one
+// warp's lanes touch for different digits fall in different banks (with stride
+// W they would share 32 / W banks).
 template <int W>
-constexpr int kHistWords = W == 1 ? 256 : 256 * (W + 1);
+constexpr int kHistStride = W == 1 ? 1 : (W % 2 == 0 ? W + 1 : W + 2);
+template <int W>
+constexpr int kHistWords = 256 * kHistStride<W>;
 template <int W>
 __device__ __forceinline__ int hidx(int d, int w) {
-    return W == 1 ? d : d * (W + 1) + w;
+    return W == 1 ? d : d * kHistStride<W> + w;
 }
 
 // SV: product values in shared memory (else in a per-CTA global slab).
@@ -68,14 +70,14 @@ struct RowSmem {
 };
 
 // Exclusive scan of the 256*W digit counters in (digit, warp) order, 8
-// consecutive counters per thread (logical index L lives at L + L / W).
+// consecutive counters per thread (logical index L = d * W + w).
 template <int W>
 __device__ inline void scan_counters(uint32_t* c, int64_t* tmp) {
     constexpr int kPer = 8;
     const int lane = threadIdx.x & 31;
     const int warp = W == 1 ? 0 : (threadIdx.x >> 5);
     const int tid = W == 1 ? lane : threadIdx.x;
-    auto phys = [](int L) { return W == 1 ? L : L + L / W; };
+    auto phys = [](int L) { return W == 1 ? L : hidx<W>(L / W, L % W); };
     uint32_t v[kPer];
     uint32_t sum = 0;
 #pragma unroll

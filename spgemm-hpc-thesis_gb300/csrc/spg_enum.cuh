@@ -51,13 +51,17 @@ __device__ inline void row_segment(const Job& J, int row, int64_t a0, bool has_s
     }
 }
 
-// Smallest j in [0, N) with incl[j] > t (the batch total exceeds t).
+__host__ __device__ constexpr int pow2_ceil_c(int x) { return x <= 1 ? 1 : 2 * pow2_ceil_c((x + 1) / 2); }
+
+// Smallest j in [0, N) with incl[j] > t (the batch total exceeds t): the
+// number of entries <= t, by binary lifting over the next power of two (the
+// bound test folds away when N is one).
 template <int N, typename Idx>
 __device__ inline int seg_search(const Idx* incl, Idx t) {
     int j = 0;
 #pragma unroll
-    for (int step = N / 2; step >= 1; step >>= 1)
-        if (incl[j + step - 1] <= t) j += step;
+    for (int step = pow2_ceil_c(N) / 2; step >= 1; step >>= 1)
+        if ((N == pow2_ceil_c(N) || j + step - 1 < N) && incl[j + step - 1] <= t) j += step;
     return j;
 }
 
