@@ -9,8 +9,9 @@ reference's definition, two_sided_spgemm.cpp:188-192).
 * value: device-resident operands, result left on the device; every timed step
   between its own CUDA events on the engine's stream; workloads whose inputs
   fit in L2 get an L2 flush between steps, outside the events.
-* e2e: the same product through the C ABI with host (pinned) buffers: the
-  host->device copy of A and the device->host copy of C inside every step.
+* e2e: the same product through the C ABI with host (pinned) buffers
+  (spg_multiply_to_host): the host->device copy of A and the device->host copy
+  of C inside every step, the copy of C overlapping the computation.
 * roofline: the numeric phase (K4, all bins), its algorithmic bytes over its
   CUDA-event time measured in every timed step.
 * cpu_baseline: the reference's OpenMP row loop (the oracle port of
@@ -361,12 +362,9 @@ def run_gpu_arm(args, rank, world, local):
         d2h = sum(8 * (a.rows + 1) + 12 * n for (a, _), n in zip(pairs, c_nnz))
 
         def e2e_step():
+            # spg_multiply_to_host: row blocks whose device->host copies overlap the later blocks
             for (pa, pb), (orp, oci, ova) in zip(host_pairs, outs):
-                r = eng.multiply(pa, pb, out="device")
-                r._engine._check(sg.library().spg_result_download(
-                    eng.h, sg.C.byref(r._res), sg.C.c_void_p(orp.data_ptr()), sg.C.c_void_p(oci.data_ptr()),
-                    sg.C.c_void_p(ova.data_ptr())))
-                r.free()
+                eng.multiply_to_host(pa, pb, orp, oci, ova)
             return float(ova[0].item()) if ova.numel() else 0.0
 
         for _ in range(max(1, args.warmup)):

@@ -117,6 +117,20 @@ void* spg_stream(spg_handle* handle);
 spg_status spg_multiply(spg_handle* handle, const spg_csr_view* A, const spg_csr_view* B, int32_t out_location,
                         spg_csr_result* C);
 
+/* C = A * B written into caller host arrays: row_ptr of A.rows+1 entries,
+ * col/val of c_capacity entries (nnz(C) <= the scalar-product count, so that
+ * count is always enough).  The product runs in row blocks of about 2^27
+ * scalar products; the device->host copy of each finished block runs on a
+ * second stream while later blocks compute, so the transfer of C overlaps the
+ * computation.  Page-locked buffers (spg_host_alloc) are needed for the
+ * overlap; pageable ones work but copy synchronously.  *c_nnz receives nnz(C);
+ * if it exceeds c_capacity the call fails with SPG_BUDGET_EXCEEDED and *c_nnz
+ * holds a lower bound of the entries needed.  Results are those of
+ * spg_multiply.  Same reference counterpart as spg_multiply: the by-value
+ * CsrMatrix return of spgemm() (spgemm_exchange.hpp:37-39). */
+spg_status spg_multiply_to_host(spg_handle* handle, const spg_csr_view* A, const spg_csr_view* B, int64_t* c_row_ptr,
+                                int32_t* c_col, double* c_val, int64_t c_capacity, int64_t* c_nnz);
+
 /* Copies a device result into caller host buffers of exactly C->rows+1 /
  * C->nnz / C->nnz elements (any of them may be NULL to skip that array). */
 spg_status spg_result_download(spg_handle* handle, const spg_csr_result* C, int64_t* row_ptr, int32_t* col,

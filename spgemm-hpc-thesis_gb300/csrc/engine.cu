@@ -40,6 +40,11 @@ struct spg_handle {
     bool acc_has = false;
     // pinned control block for small device->host reads
     void* ctrl = nullptr;
+    // spg_multiply_to_host: copies of finished row blocks run on their own stream
+    cudaStream_t copy_stream = nullptr;
+    // page-locked staging for per-product reads of batches (grown on demand)
+    void* host_scratch = nullptr;
+    size_t host_scratch_bytes = 0;
 };
 
 namespace {
@@ -98,6 +103,21 @@ private:
 };
 
 void sync(spg_handle* h) { check_cuda(cudaStreamSynchronize(h->stream), "cudaStreamSynchronize"); }
+
+// Page-locked host staging of at least `bytes` (control reads go through
+// launch_readback into it, never through a copy engine).
+void* host_staging(spg_handle* h, size_t bytes) {
+    if (bytes > h->host_scratch_bytes) {
+        sync(h);
+        if (h->host_scratch) cudaFreeHost(h->host_scratch);
+        h->host_scratch = nullptr;
+        h->host_scratch_bytes = 0;
+        const size_t want = std::max<size_t>(bytes, 64 << 10);
+        check_cuda(cudaMallocHost(&h->host_scratch, want), "host staging");
+        h->host_scratch_bytes = want;
+    }
+    return h->host_scratch;
+}
 
 void require(bool ok, spg_status s, const std::string& msg) {
     if (!ok) throw Failure{s, msg};
@@ -166,6 +186,8 @@ struct Ctrl {  // layout of the pinned control block and its device twin
     unsigned long long cursor[kNumBins];
     int64_t totals[2];  // scanned totals (symbolic, numeric)
 };
+
+static_assert(sizeof(Ctrl) % 8 == 0 && sizeof(Ctrl) <= 4096, "Ctrl is read back in 8-byte words into kCtrlBytes");
 
 spg_status map_err(const ErrWord& e, std::string& msg) {
     char buf[160];
@@ -265,15 +287,19 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
     check_cuda(cudaGetLastError(), "K1 launch");
     cudaEventRecord(h->ev[1], st);
     std::vector<int64_t> job_products(njobs, 0);
+    int64_t* h_jp = nullptr;
     if (njobs > 1) {
         int64_t* d_jp = ar.alloc<int64_t>(static_cast<size_t>(njobs), "job products");
+        h_jp = static_cast<int64_t*>(host_staging(h, sizeof(int64_t) * njobs));
         launch_job_products(d_jobs, njobs, d_row_base, d_jp, st);
-        ++launches;
-        check_cuda(cudaMemcpyAsync(job_products.data(), d_jp, sizeof(int64_t) * njobs, cudaMemcpyDeviceToHost, st),
-                   "D2H job products");
+        launch_readback(d_jp, h_jp, sizeof(int64_t) * njobs, st);
+        launches += 2;
     }
-    check_cuda(cudaMemcpyAsync(hc, d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, st), "D2H ctrl");
+    launch_readback(d_ctrl, hc, sizeof(Ctrl), st);
+    ++launches;
+    check_cuda(cudaGetLastError(), "readback launch");
     sync(h);  // sync 1: bins and input checks
+    if (h_jp) std::copy(h_jp, h_jp + njobs, job_products.begin());
     if (hc->err.code) {
         std::string msg;
         const spg_status s = map_err(hc->err, msg);
@@ -317,9 +343,9 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
     check_cuda(cudaGetLastError(), "K3 launch");
     cudaEventRecord(h->ev[3], st);
     if (exact) {
-        check_cuda(cudaMemcpyAsync(&hc->totals[0], cnt + slots - 1, sizeof(int64_t), cudaMemcpyDeviceToHost, st),
-                   "D2H total");
-        check_cuda(cudaMemcpyAsync(&hc->err, &d_ctrl->err, sizeof(ErrWord), cudaMemcpyDeviceToHost, st), "D2H err");
+        launch_readback(cnt + slots - 1, &hc->totals[0], sizeof(int64_t), st);
+        launch_readback(&d_ctrl->err, &hc->err, sizeof(ErrWord), st);
+        launches += 2;
         sync(h);  // exact mode: size of C
         if (hc->err.code) {
             std::string msg;
@@ -346,7 +372,8 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
     }
     check_cuda(cudaGetLastError(), "K4 launch");
     cudaEventRecord(h->ev[4], st);
-    check_cuda(cudaMemcpyAsync(hc, d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, st), "D2H ctrl");
+    launch_readback(d_ctrl, hc, sizeof(Ctrl), st);
+    ++launches;
     sync(h);  // stored count and errors
     if (hc->err.code) {
         std::string msg;
@@ -385,10 +412,11 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
         check_cuda(cudaMemcpyAsync(d_idx, idx.data(), sizeof(int64_t) * njobs, cudaMemcpyHostToDevice, st),
                    "H2D start index");
         launch_gather(final_rp, d_idx, d_starts, njobs, st);
-        launches += 2;  // gather + rebase
-        check_cuda(cudaMemcpyAsync(starts.data(), d_starts, sizeof(int64_t) * njobs, cudaMemcpyDeviceToHost, st),
-                   "D2H starts");
+        int64_t* h_starts = static_cast<int64_t*>(host_staging(h, sizeof(int64_t) * njobs));
+        launch_readback(d_starts, h_starts, sizeof(int64_t) * njobs, st);
+        launches += 3;  // gather + readback + rebase
         sync(h);
+        std::copy(h_starts, h_starts + njobs, starts.begin());
     }
     out.resize(njobs);
     for (int j = 0; j < njobs; ++j) {
@@ -574,6 +602,11 @@ void spg_destroy(spg_handle* h) {
     cudaSetDevice(h->device);
     if (h->acc_has) free_result_arrays(h, &h->acc);
     cudaStreamSynchronize(h->stream);
+    if (h->copy_stream) {
+        cudaStreamSynchronize(h->copy_stream);
+        cudaStreamDestroy(h->copy_stream);
+    }
+    if (h->host_scratch) cudaFreeHost(h->host_scratch);
     for (auto& e : h->ev) cudaEventDestroy(e);
     for (auto& e : h->bin_ev) cudaEventDestroy(e);
     cudaStreamDestroy(h->stream);
@@ -610,6 +643,126 @@ spg_status spg_multiply(spg_handle* h, const spg_csr_view* A, const spg_csr_view
         std::vector<DevResult> out;
         run_products(h, in, out, false, nullptr);
         deliver(h, out[0], out_location, C);
+    });
+}
+
+// Row blocks of about kChunkProducts scalar products each (at most kMaxChunks).
+constexpr int64_t kChunkProducts = int64_t{1} << 27;
+constexpr int kMaxChunks = 16;
+
+spg_status spg_multiply_to_host(spg_handle* h, const spg_csr_view* A, const spg_csr_view* B, int64_t* c_row_ptr,
+                                int32_t* c_col, double* c_val, int64_t c_capacity, int64_t* c_nnz) {
+    return guarded(h, [&] {
+        require(A && B && c_row_ptr && c_nnz && c_capacity >= 0 && (c_capacity == 0 || (c_col && c_val)),
+                SPG_INVALID_ARGUMENT, "bad spg_multiply_to_host arguments");
+        check_view(A, "A");
+        check_view(B, "B");
+        require(A->cols == B->rows, SPG_INVALID_ARGUMENT, "SpGEMM requires A.cols == B.rows");
+        *c_nnz = 0;
+        if (!h->copy_stream)
+            check_cuda(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking), "copy stream");
+        cudaStream_t st = h->stream, cs = h->copy_stream;
+        // operands on the device once for all row blocks
+        Arena ar(h);
+        const spg_csr_view* views[2] = {A, B};
+        spg_csr_view dv[2];
+        for (int i = 0; i < 2; ++i) {
+            dv[i] = *views[i];
+            if (views[i]->location == SPG_HOST) {
+                const bool same = i == 1 && B->row_ptr == A->row_ptr && B->col == A->col && B->val == A->val &&
+                                  B->rows == A->rows && B->cols == A->cols && B->nnz == A->nnz;
+                const CsrView v = same ? CsrView{} : stage(h, ar, views[i]);
+                if (same) dv[1] = dv[0];
+                else {
+                    dv[i].row_ptr = v.rp;
+                    dv[i].col = v.ci;
+                    dv[i].val = v.v;
+                    dv[i].location = SPG_DEVICE;
+                }
+            }
+        }
+        // row blocks: equal numbers of rows, about kChunkProducts products each
+        int64_t products = 0;
+        {
+            std::vector<JobIn> in{{&dv[0], &dv[1], CsrView{}}};
+            std::vector<DevResult> none;
+            run_products(h, in, none, true, &products);
+        }
+        const int32_t m = A->rows;
+        const int nchunks = static_cast<int>(
+            std::max<int64_t>(1, std::min<int64_t>({kMaxChunks, (products + kChunkProducts - 1) / kChunkProducts,
+                                                    static_cast<int64_t>(m)})));
+        spg_timings sum{};
+        int64_t off = 0;
+        std::vector<cudaEvent_t> done;
+        // Block results stay allocated until every copy has finished: memory freed
+        // on the copy stream and reused by the compute stream would make the
+        // compute wait for the copies (the pool orders reuse after the free).
+        std::vector<DevResult> held;
+        auto release_held = [&] {
+            for (auto& q : held) {
+                cudaFreeAsync(q.rp, st);
+                cudaFreeAsync(q.ci, st);
+                cudaFreeAsync(q.v, st);
+            }
+            held.clear();
+        };
+        c_row_ptr[0] = 0;
+        for (int k = 0; k < nchunks; ++k) {
+            const int32_t r0 = static_cast<int32_t>(static_cast<int64_t>(m) * k / nchunks);
+            const int32_t r1 = static_cast<int32_t>(static_cast<int64_t>(m) * (k + 1) / nchunks);
+            spg_csr_view blk = dv[0];
+            blk.rows = r1 - r0;
+            blk.row_ptr = dv[0].row_ptr + r0;  // absolute offsets into A's column/value arrays
+            std::vector<JobIn> in{{&blk, &dv[1], CsrView{}}};
+            std::vector<DevResult> out;
+            run_products(h, in, out, false, nullptr);
+            DevResult& r = out[0];
+            if (off + r.nnz > c_capacity) {
+                held.push_back(r);
+                cudaStreamSynchronize(cs);
+                release_held();
+                for (auto e : done) cudaEventDestroy(e);
+                *c_nnz = off + r.nnz;  // at least this many entries are needed
+                throw Failure{SPG_BUDGET_EXCEEDED, "nnz(C) exceeds c_capacity"};
+            }
+            // this block's offsets continue the previous ones; copy it out on the copy stream
+            launch_add_offset(r.rp + 1, r.rows, off, st);
+            cudaEvent_t e;
+            check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+            check_cuda(cudaEventRecord(e, st), "event record");
+            check_cuda(cudaStreamWaitEvent(cs, e, 0), "stream wait");
+            check_cuda(cudaMemcpyAsync(c_row_ptr + r0 + 1, r.rp + 1, sizeof(int64_t) * r.rows, cudaMemcpyDeviceToHost, cs),
+                       "D2H row_ptr");
+            if (r.nnz) {
+                check_cuda(cudaMemcpyAsync(c_col + off, r.ci, sizeof(int32_t) * r.nnz, cudaMemcpyDeviceToHost, cs),
+                           "D2H col");
+                check_cuda(cudaMemcpyAsync(c_val + off, r.v, sizeof(double) * r.nnz, cudaMemcpyDeviceToHost, cs),
+                           "D2H val");
+            }
+            held.push_back(r);
+            done.push_back(e);
+            off += r.nnz;
+            sum.ms_rowwork += h->last.ms_rowwork;
+            sum.ms_symbolic += h->last.ms_symbolic;
+            sum.ms_scan += h->last.ms_scan;
+            sum.ms_numeric += h->last.ms_numeric;
+            sum.ms_compact += h->last.ms_compact;
+            sum.ms_total += h->last.ms_total;
+            sum.launches += h->last.launches + 1;
+            for (int b = 0; b < kNumBins; ++b) {
+                sum.bin_rows[b] += h->last.bin_rows[b];
+                sum.ms_numeric_bin[b] += h->last.ms_numeric_bin[b];
+            }
+        }
+        check_cuda(cudaStreamSynchronize(cs), "copy stream");
+        release_held();
+        for (auto e : done) cudaEventDestroy(e);
+        *c_nnz = off;
+        sum.products = products;
+        sum.nnz = off;
+        sum.rows = m;
+        h->last = sum;
     });
 }
 

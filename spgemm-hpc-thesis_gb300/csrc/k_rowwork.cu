@@ -264,6 +264,18 @@ __global__ void gather_kernel(const int64_t* __restrict__ src, const int64_t* __
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[idx[i]];
 }
 
+// Small device->host reads by a kernel storing into mapped page-locked memory:
+// they do not queue on the copy engines behind bulk result copies.
+__global__ void readback_kernel(const unsigned long long* __restrict__ src, unsigned long long* dst, int64_t words) {
+    for (int64_t i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
+}
+
+__global__ void add_offset_kernel(int64_t* __restrict__ d, int64_t n, int64_t add) {
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        d[i] += add;
+}
+
 // One CTA per product: its scalar products, the sum of its rows' ub.
 __global__ void job_products_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ job_row_base,
                                     int64_t* __restrict__ out) {
@@ -354,6 +366,17 @@ void launch_job_products(const Job* d_jobs, int njobs, const int64_t* d_job_row_
                          cudaStream_t stream) {
     if (njobs <= 0) return;
     job_products_kernel<<<njobs, 256, 0, stream>>>(d_jobs, d_job_row_base, d_out);
+}
+
+void launch_readback(const void* d_src, void* h_dst, size_t bytes, cudaStream_t stream) {
+    if (bytes == 0) return;
+    readback_kernel<<<1, 256, 0, stream>>>(static_cast<const unsigned long long*>(d_src),
+                                           static_cast<unsigned long long*>(h_dst), static_cast<int64_t>(bytes / 8));
+}
+
+void launch_add_offset(int64_t* d, int64_t n, int64_t add, cudaStream_t stream) {
+    if (n <= 0 || add == 0) return;
+    add_offset_kernel<<<grid_for(n, 256, 152 * 8), 256, 0, stream>>>(d, n, add);
 }
 
 void launch_rebase(const RebaseItem* d_items, int n, int64_t max_rows, cudaStream_t stream) {

@@ -214,6 +214,11 @@ struct RebaseItem {
 };
 void launch_gather(const int64_t* d_src, const int64_t* d_idx, int64_t* d_dst, int n, cudaStream_t stream);
 void launch_rebase(const RebaseItem* d_items, int n, int64_t max_rows, cudaStream_t stream);
+// Copies `bytes` (a multiple of 8, 8-byte aligned) from device memory into
+// page-locked host memory with a kernel (no copy engine involved).
+void launch_readback(const void* d_src, void* h_dst, size_t bytes, cudaStream_t stream);
+// d[i] += add for i < n.
+void launch_add_offset(int64_t* d, int64_t n, int64_t add, cudaStream_t stream);
 // Scalar products of every product of a batch (after K1): out[j] = sum of job j's ub.
 void launch_job_products(const Job* d_jobs, int njobs, const int64_t* d_job_row_base, int64_t* d_out,
                          cudaStream_t stream);

@@ -138,7 +138,7 @@ def library() -> C.CDLL:
         lib.spg_server_destroy.restype = None
         for name in ("spg_multiply", "spg_multiply_batch", "spg_accum_begin", "spg_accum_add", "spg_accum_finish",
                      "spg_result_download", "spg_result_free", "spg_scalar_multiplication_count",
-                     "spg_scalar_multiplication_count_batch", "spg_last_timings", "spg_create",
+                     "spg_scalar_multiplication_count_batch", "spg_last_timings", "spg_create", "spg_multiply_to_host",
                      "spg_config_default", "spg_server_create", "spg_submit", "spg_poll", "spg_cancel",
                      "spg_server_result_free"):
             getattr(lib, name).restype = C.c_int
@@ -257,6 +257,23 @@ class Engine:
         loc = SPG_DEVICE if out == "device" else SPG_HOST
         self._check(library().spg_multiply(self.h, C.byref(va), C.byref(vb), C.c_int32(loc), C.byref(res)))
         return DeviceResult(self, res) if loc == SPG_DEVICE else _take_host(res, self)
+
+    def multiply_to_host(self, a, b, row_ptr, col, val) -> int:
+        """C = A * B into caller host arrays (numpy or pinned torch CPU tensors:
+        row_ptr int64[A.rows+1], col int32[cap], val float64[cap]); returns
+        nnz(C).  Device->host copies of finished row blocks overlap the rest."""
+        keep: list = []
+        va, vb = _view(a, keep), _view(b, keep)
+
+        def ptr(x):
+            return x.data_ptr() if hasattr(x, "data_ptr") else x.ctypes.data
+
+        cap = min(len(col), len(val))
+        nnz = C.c_int64()
+        self._check(library().spg_multiply_to_host(self.h, C.byref(va), C.byref(vb), C.c_void_p(ptr(row_ptr)),
+                                                   C.c_void_p(ptr(col)), C.c_void_p(ptr(val)), C.c_int64(cap),
+                                                   C.byref(nnz)))
+        return nnz.value
 
     def multiply_batch(self, pairs, out: str = "host") -> list:
         keep: list = []
