@@ -380,6 +380,25 @@ def run_gpu_arm(args, rank, world, local):
         e2e = {"value": 2.0 * all_sum(products * ke, world) / te / 1e9, "unit": "GFLOP/s",
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": ke}
 
+    # plan replay: the same products with their structure phases done once and the
+    # value phases (numeric, scan, compaction) replayed as one CUDA graph per step
+    replay = None
+    if not args.no_replay:
+        with eng.plan(dev_pairs) as plan:
+            for _ in range(args.warmup):
+                plan.execute()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            dev_ms = 0.0
+            for _ in range(args.steps):
+                plan.execute()
+                dev_ms += plan.last_ms
+            wall = time.perf_counter() - t0
+        replay = {"value": 2.0 * products * args.steps / wall / 1e9, "unit": "GFLOP/s",
+                  "ms_per_step": 1e3 * wall / args.steps, "device_ms_per_step": dev_ms / args.steps,
+                  "what": "spg_plan_execute: numeric + scan + compaction of the same products replayed as one "
+                          "CUDA graph per step; row work, bins and allocation done once at plan time"}
+
     pk = peaks()
     numeric_avg_s = numeric_ms / args.steps / 1e3
     achieved = bytes_alg / numeric_avg_s / 1e9 if numeric_avg_s > 0 else None
@@ -414,7 +433,7 @@ def run_gpu_arm(args, rank, world, local):
                               else f"inputs larger than L2 ({in_bytes / 1e6:.0f} MB, no flush)"),
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-            "gpu_launches": int(launches), "clocks": clocks.summary(),
+            "gpu_launches": int(launches), "clocks": clocks.summary(), "graph_replay": replay,
             "phases_ms_last_step": {k: v for k, v in eng.last_timings().items()
                                     if k.startswith("ms_")},
         }
@@ -593,6 +612,21 @@ def run_served(args, rank, world, local):
                     n = int(min(400, max(100, 3 * rate)))
                     at, picks = _arrivals(rate, n, len(pool), seed=rate)
                     table[mode][str(rate)] = _serve_trace(srv, dev, products, at, picks)
+    # the whole pool as one plan: all 24 requests per CUDA-graph replay
+    eng = sg.Engine(local)
+    with eng.plan(dev) as plan:
+        for _ in range(3):
+            plan.execute()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        reps = 10
+        for _ in range(reps):
+            plan.execute()
+        wall = time.perf_counter() - t0
+    eng.close()
+    replay = {"req_per_s": reps * len(pool) / wall, "gflops": 2.0 * sum(products) * reps / wall / 1e9,
+              "what": "the 24 pool requests as one spg_plan: value phases replayed as one CUDA graph per "
+                      "24 requests (structure phases at plan time)"}
     sat_b, sat_p = table["batched"]["saturation"], table["per_request"]["saturation"]
     line = {
         "metric": "served products/s", "value": sat_b["req_per_s"], "unit": "products/s", "n_gpus": world,
@@ -607,7 +641,7 @@ def run_served(args, rank, world, local):
                                  "p50_ms": sat_p["p50_ms"], "p99_ms": sat_p["p99_ms"]},
         "batched_over_per_request": sat_b["req_per_s"] / sat_p["req_per_s"],
         "p50_ms": sat_b["p50_ms"], "p99_ms": sat_b["p99_ms"],
-        "by_rate": table, "roofline": None, "cpu_baseline": None, "e2e": None,
+        "by_rate": table, "graph_replay": replay, "roofline": None, "cpu_baseline": None, "e2e": None,
         "gpu_launches": int(sum(v["launches"] for m in table.values() for v in m.values())),
         "clocks": clocks.summary(),
     }
@@ -648,6 +682,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-replay", action="store_true", help="skip the plan-replay (CUDA graph) sub-measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

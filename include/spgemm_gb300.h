@@ -178,6 +178,32 @@ spg_status spg_multiply_batch(spg_handle* handle, int32_t n, const spg_csr_view*
 spg_status spg_scalar_multiplication_count_batch(spg_handle* handle, int32_t n, const spg_csr_view* A,
                                                  const spg_csr_view* B, int64_t* products);
 
+/* ---- plans: one sparsity structure, many value sets ------------------------------
+ * No reference counterpart.  For products whose operands keep their structure
+ * (row offsets and columns) while their values change -- a Galerkin product
+ * re-formed after the fine operator's coefficients change, Trident's
+ * repeated stage products -- spg_plan_create runs the structure-dependent
+ * phases once (row work, bins, upper-bound offsets, every allocation) for the
+ * n device-resident products A[i] * B[i], and captures the value-dependent
+ * phases (numeric, scan, compaction, per-product offsets) as one CUDA graph.
+ * spg_plan_execute replays the graph on the handle's stream with the values
+ * the operand arrays hold at that time, waits for it and writes nnz(C_i) to
+ * nnz[i] (nnz may be NULL).  Results equal spg_multiply's bit for bit.  The
+ * operand arrays must stay valid and keep their structure for the plan's
+ * life.  A plan holds 24 bytes per scalar product plus 40 per row.
+ * spg_plan_result gives a device view of product i of the last execution
+ * (memory owned by the plan: valid until the next execute or destroy; do not
+ * pass it to spg_result_free).  spg_plan_last_ms: device time of the last
+ * execution.  A handle's plans and calls share its stream: do not use them
+ * from different threads at once. */
+typedef struct spg_plan spg_plan;
+spg_status spg_plan_create(spg_handle* handle, int32_t n, const spg_csr_view* A, const spg_csr_view* B,
+                           spg_plan** plan);
+spg_status spg_plan_execute(spg_plan* plan, int64_t* nnz);
+spg_status spg_plan_result(const spg_plan* plan, int32_t i, spg_csr_result* C);
+float spg_plan_last_ms(const spg_plan* plan);
+void spg_plan_destroy(spg_plan* plan);
+
 /* ---- serving loop ---------------------------------------------------------------
  * No reference counterpart (the reference runs one product per call).  A
  * server accepts products as they arrive and runs them in batches on one GPU:

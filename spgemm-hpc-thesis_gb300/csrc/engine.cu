@@ -902,6 +902,239 @@ spg_status spg_multiply_batch(spg_handle* h, int32_t n, const spg_csr_view* A, c
     });
 }
 
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Plans: the structure-dependent phases once, the value-dependent phases as a
+// CUDA graph replayed by spg_plan_execute.
+struct spg_plan {
+    spg_handle* h = nullptr;
+    int njobs = 0;
+    std::vector<int64_t> row_base;     // njobs + 1
+    std::vector<int32_t> rows, cols;
+    std::vector<int64_t> job_products;
+    std::vector<void*> bufs;           // device allocations owned by the plan
+    int64_t* rp = nullptr;             // per-product offsets (rebased), slots entries
+    int32_t* col = nullptr;
+    double* val = nullptr;
+    Ctrl* hc = nullptr;                // page-locked readbacks
+    int64_t* h_starts = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool executed = false;
+    int64_t nz_total = 0;
+    std::vector<int64_t> starts;       // njobs + 1
+    float ms_last = 0.0f;
+};
+
+namespace {
+
+template <typename T>
+T* plan_alloc(spg_plan* p, size_t count, const char* what) {
+    void* q = nullptr;
+    check_cuda(cudaMalloc(&q, std::max<size_t>(count * sizeof(T), 16)), what);
+    p->bufs.push_back(q);
+    return static_cast<T*>(q);
+}
+
+void plan_free(spg_plan* p) {
+    if (!p) return;
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    for (void* q : p->bufs) cudaFree(q);
+    if (p->hc) cudaFreeHost(p->hc);
+    if (p->h_starts) cudaFreeHost(p->h_starts);
+    delete p;
+}
+
+void plan_build(spg_plan* p, int32_t n, const spg_csr_view* A, const spg_csr_view* B) {
+    spg_handle* h = p->h;
+    cudaStream_t st = h->stream;
+    p->njobs = n;
+    p->row_base.assign(n + 1, 0);
+    std::vector<Job> jobs(n);
+    for (int j = 0; j < n; ++j) {
+        check_view(&A[j], "A");
+        check_view(&B[j], "B");
+        require(A[j].location == SPG_DEVICE && B[j].location == SPG_DEVICE, SPG_INVALID_ARGUMENT,
+                "a plan needs device-resident operands");
+        require(A[j].cols == B[j].rows, SPG_INVALID_ARGUMENT, "SpGEMM requires A.cols == B.rows");
+        p->row_base[j + 1] = p->row_base[j] + A[j].rows;
+        p->rows.push_back(A[j].rows);
+        p->cols.push_back(B[j].cols);
+        auto view = [](const spg_csr_view& m) {
+            CsrView v;
+            v.rows = m.rows;
+            v.cols = m.cols;
+            v.nnz = m.nnz;
+            v.rp = m.row_ptr;
+            v.ci = m.col;
+            v.v = m.val;
+            return v;
+        };
+        jobs[j].A = view(A[j]);
+        jobs[j].B = view(B[j]);
+        jobs[j].row_base = p->row_base[j];
+    }
+    const int64_t total_rows = p->row_base[n];
+    const size_t slots = static_cast<size_t>(total_rows + n);
+    int64_t* ub = plan_alloc<int64_t>(p, static_cast<size_t>(total_rows), "plan ub");
+    int64_t* cnt = plan_alloc<int64_t>(p, slots, "plan cnt");
+    int64_t* nz = plan_alloc<int64_t>(p, slots, "plan nz");
+    int64_t* items = plan_alloc<int64_t>(p, static_cast<size_t>(total_rows), "plan items");
+    int64_t* d_row_base = plan_alloc<int64_t>(p, static_cast<size_t>(n) + 1, "plan row_base");
+    Ctrl* d_ctrl = plan_alloc<Ctrl>(p, 1, "plan ctrl");
+    Job* d_jobs = plan_alloc<Job>(p, static_cast<size_t>(n), "plan jobs");
+    int64_t* d_jp = plan_alloc<int64_t>(p, static_cast<size_t>(n), "plan job products");
+    for (int j = 0; j < n; ++j) {
+        jobs[j].ub = ub + p->row_base[j];
+        jobs[j].cnt = cnt + p->row_base[j] + j;
+        jobs[j].nz = nz + p->row_base[j] + j;
+        jobs[j].holes = 1;
+    }
+    check_cuda(cudaMallocHost(reinterpret_cast<void**>(&p->hc), sizeof(Ctrl)), "plan host ctrl");
+    check_cuda(cudaMallocHost(reinterpret_cast<void**>(&p->h_starts), sizeof(int64_t) * (n + 1)), "plan host starts");
+    check_cuda(cudaMemsetAsync(cnt, 0, slots * sizeof(int64_t), st), "memset");
+    check_cuda(cudaMemsetAsync(d_ctrl, 0, sizeof(Ctrl), st), "memset");
+    check_cuda(cudaMemcpyAsync(d_row_base, p->row_base.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, st),
+               "H2D");
+    check_cuda(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(Job) * n, cudaMemcpyHostToDevice, st), "H2D");
+    // structure: row work, bins, the upper-bound offsets
+    launch_rowwork(d_jobs, n, d_row_base, total_rows, &d_ctrl->stats, &d_ctrl->err, st);
+    launch_bin_offsets(&d_ctrl->stats, d_ctrl->bin_off, st);
+    launch_bin_scatter(d_jobs, n, d_row_base, total_rows, d_ctrl->bin_off, d_ctrl->cursor, items, st);
+    launch_job_products(d_jobs, n, d_row_base, d_jp, st);
+    int64_t* partials = plan_alloc<int64_t>(p, scan_partials_count(static_cast<int64_t>(slots)), "plan partials");
+    launch_scan(cnt, static_cast<int64_t>(slots) - 1, partials, st);
+    launch_readback(d_ctrl, p->hc, sizeof(Ctrl), st);
+    check_cuda(cudaGetLastError(), "plan structure launches");
+    p->job_products.assign(n, 0);
+    check_cuda(cudaMemcpyAsync(p->job_products.data(), d_jp, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, st), "D2H");
+    sync(h);
+    if (p->hc->err.code) {
+        std::string msg;
+        const spg_status s = map_err(p->hc->err, msg);
+        throw Failure{s, msg};
+    }
+    const int64_t products = static_cast<int64_t>(p->hc->stats.products);
+    const int64_t max_ub = static_cast<int64_t>(p->hc->stats.max_ub);
+    require(max_ub < (int64_t{1} << 30), SPG_OVERFLOW, "an output row has more than 2^30 scalar products (engine limit)");
+    int64_t bin_count[kNumBins], bin_off[kNumBins + 1];
+    for (int b = 0; b < kNumBins; ++b) bin_count[b] = static_cast<int64_t>(p->hc->stats.bin_count[b]);
+    for (int b = 0; b <= kNumBins; ++b) bin_off[b] = p->hc->bin_off[b];
+    if (h->cfg.hbm_budget_bytes)
+        require(static_cast<uint64_t>(products) * 24 <= h->cfg.hbm_budget_bytes, SPG_BUDGET_EXCEEDED,
+                "plan footprint exceeds the handle's HBM budget");
+    int32_t* tmp_col = plan_alloc<int32_t>(p, static_cast<size_t>(products), "plan C_tmp col");
+    double* tmp_val = plan_alloc<double>(p, static_cast<size_t>(products), "plan C_tmp val");
+    for (int j = 0; j < n; ++j) {
+        jobs[j].c_col = tmp_col;
+        jobs[j].c_val = tmp_val;
+    }
+    check_cuda(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(Job) * n, cudaMemcpyHostToDevice, st), "H2D");
+    const size_t scratch_bytes = numeric_scratch_bytes(bin_count, max_ub, h->num_sms, true);
+    void* scratch = scratch_bytes ? plan_alloc<unsigned char>(p, scratch_bytes, "plan scratch") : nullptr;
+    p->col = plan_alloc<int32_t>(p, static_cast<size_t>(products), "plan C col");
+    p->val = plan_alloc<double>(p, static_cast<size_t>(products), "plan C val");
+    p->rp = plan_alloc<int64_t>(p, slots, "plan C row_ptr");
+    std::vector<int64_t> idx(n);
+    for (int j = 0; j < n; ++j) idx[j] = p->row_base[j] + j;
+    int64_t* d_idx = plan_alloc<int64_t>(p, static_cast<size_t>(n), "plan start index");
+    int64_t* d_starts = plan_alloc<int64_t>(p, static_cast<size_t>(n), "plan starts");
+    check_cuda(cudaMemcpyAsync(d_idx, idx.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, st), "H2D");
+    sync(h);  // idx, jobs copied
+    int64_t max_rows = 0;
+    for (int32_t r : p->rows) max_rows = std::max<int64_t>(max_rows, r);
+
+    // values: the replayed part
+    check_cuda(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed), "begin capture");
+    cudaMemsetAsync(nz, 0, slots * sizeof(int64_t), st);
+    cudaMemsetAsync(d_ctrl, 0, sizeof(Ctrl), st);
+    for (int b = 1; b < kNumBins; ++b)
+        if (bin_count[b])
+            launch_numeric(b, d_jobs, items + bin_off[b], bin_count[b], max_ub, scratch, scratch_bytes,
+                           &d_ctrl->stats, &d_ctrl->err, st, h->num_sms, true);
+    launch_scan(nz, static_cast<int64_t>(slots) - 1, partials, st);
+    launch_compact_holes(d_jobs, n, d_row_base, total_rows, p->col, p->val, st);
+    launch_gather(nz, d_idx, d_starts, n, st);
+    launch_rebase_jobs(nz, p->rp, d_row_base, n, max_rows, st);
+    launch_readback(d_starts, p->h_starts, sizeof(int64_t) * n, st);
+    launch_readback(d_ctrl, p->hc, sizeof(Ctrl), st);
+    const cudaError_t le = cudaGetLastError();
+    const cudaError_t ce = cudaStreamEndCapture(st, &p->graph);
+    check_cuda(le, "plan capture launches");
+    check_cuda(ce, "end capture");
+    check_cuda(cudaGraphInstantiate(&p->exec, p->graph, 0), "graph instantiate");
+}
+
+}  // namespace
+
+extern "C" {
+
+spg_status spg_plan_create(spg_handle* h, int32_t n, const spg_csr_view* A, const spg_csr_view* B, spg_plan** plan) {
+    return guarded(h, [&] {
+        require(plan && n >= 1 && A && B, SPG_INVALID_ARGUMENT, "bad plan arguments");
+        *plan = nullptr;
+        auto* p = new spg_plan;
+        p->h = h;
+        try {
+            plan_build(p, n, A, B);
+        } catch (...) {
+            cudaStreamSynchronize(h->stream);
+            plan_free(p);
+            throw;
+        }
+        *plan = p;
+    });
+}
+
+spg_status spg_plan_execute(spg_plan* p, int64_t* nnz) {
+    if (!p) return SPG_INVALID_ARGUMENT;
+    spg_handle* h = p->h;
+    return guarded(h, [&] {
+        cudaEventRecord(h->ev[0], h->stream);
+        check_cuda(cudaGraphLaunch(p->exec, h->stream), "graph launch");
+        cudaEventRecord(h->ev[5], h->stream);
+        sync(h);
+        if (p->hc->err.code) {
+            std::string msg;
+            const spg_status s = map_err(p->hc->err, msg);
+            throw Failure{s, msg};
+        }
+        p->nz_total = static_cast<int64_t>(p->hc->stats.nz_total);
+        p->starts.assign(p->njobs + 1, 0);
+        for (int j = 0; j < p->njobs; ++j) p->starts[j] = p->h_starts[j];
+        p->starts[p->njobs] = p->nz_total;
+        p->executed = true;
+        p->ms_last = elapsed(h->ev[0], h->ev[5]);
+        if (nnz)
+            for (int j = 0; j < p->njobs; ++j) nnz[j] = p->starts[j + 1] - p->starts[j];
+    });
+}
+
+spg_status spg_plan_result(const spg_plan* p, int32_t i, spg_csr_result* C) {
+    if (!p || !C || i < 0 || i >= p->njobs || !p->executed) return SPG_INVALID_ARGUMENT;
+    std::memset(C, 0, sizeof(*C));
+    C->rows = p->rows[i];
+    C->cols = p->cols[i];
+    C->nnz = p->starts[i + 1] - p->starts[i];
+    C->row_ptr = p->rp + p->row_base[i] + i;
+    C->col = p->col + p->starts[i];
+    C->val = p->val + p->starts[i];
+    C->location = SPG_DEVICE;
+    C->products = p->job_products[i];
+    return SPG_OK;
+}
+
+float spg_plan_last_ms(const spg_plan* p) { return p ? p->ms_last : 0.0f; }
+
+void spg_plan_destroy(spg_plan* p) {
+    if (!p) return;
+    cudaSetDevice(p->h->device);
+    cudaStreamSynchronize(p->h->stream);
+    plan_free(p);
+}
+
 void* spg_host_alloc(size_t bytes) {
     void* p = nullptr;
     if (cudaMallocHost(&p, bytes ? bytes : 16) != cudaSuccess) {

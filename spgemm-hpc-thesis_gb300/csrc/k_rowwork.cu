@@ -276,6 +276,20 @@ __global__ void add_offset_kernel(int64_t* __restrict__ d, int64_t n, int64_t ad
         d[i] += add;
 }
 
+// blockIdx.y selects product j: out[base_j + r] = scanned[base_j + r] - scanned[base_j]
+// for r <= rows_j, where base_j = job_row_base[j] + j (each product's offsets
+// restart at zero; the start stays in device memory).
+__global__ void rebase_jobs_kernel(const int64_t* __restrict__ scanned, int64_t* __restrict__ out,
+                                   const int64_t* __restrict__ job_row_base) {
+    const int j = blockIdx.y;
+    const int64_t base = job_row_base[j] + j;
+    const int64_t rows = job_row_base[j + 1] - job_row_base[j];
+    const int64_t start = scanned[base];
+    for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r <= rows;
+         r += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        out[base + r] = scanned[base + r] - start;
+}
+
 // One CTA per product: its scalar products, the sum of its rows' ub.
 __global__ void job_products_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ job_row_base,
                                     int64_t* __restrict__ out) {
@@ -372,6 +386,13 @@ void launch_readback(const void* d_src, void* h_dst, size_t bytes, cudaStream_t 
     if (bytes == 0) return;
     readback_kernel<<<1, 256, 0, stream>>>(static_cast<const unsigned long long*>(d_src),
                                            static_cast<unsigned long long*>(h_dst), static_cast<int64_t>(bytes / 8));
+}
+
+void launch_rebase_jobs(const int64_t* d_scanned, int64_t* d_out, const int64_t* d_job_row_base, int njobs,
+                        int64_t max_rows, cudaStream_t stream) {
+    if (njobs <= 0) return;
+    const dim3 grid(grid_for(max_rows + 1, 256, 64), static_cast<unsigned>(njobs));
+    rebase_jobs_kernel<<<grid, 256, 0, stream>>>(d_scanned, d_out, d_job_row_base);
 }
 
 void launch_add_offset(int64_t* d, int64_t n, int64_t add, cudaStream_t stream) {

@@ -217,6 +217,10 @@ void launch_rebase(const RebaseItem* d_items, int n, int64_t max_rows, cudaStrea
 // Copies `bytes` (a multiple of 8, 8-byte aligned) from device memory into
 // page-locked host memory with a kernel (no copy engine involved).
 void launch_readback(const void* d_src, void* h_dst, size_t bytes, cudaStream_t stream);
+// Per-product row offsets restarting at zero, from offsets scanned across a
+// batch (product j's rows + 1 entries start at job_row_base[j] + j in both).
+void launch_rebase_jobs(const int64_t* d_scanned, int64_t* d_out, const int64_t* d_job_row_base, int njobs,
+                        int64_t max_rows, cudaStream_t stream);
 // d[i] += add for i < n.
 void launch_add_offset(int64_t* d, int64_t n, int64_t add, cudaStream_t stream);
 // Scalar products of every product of a batch (after K1): out[j] = sum of job j's ub.

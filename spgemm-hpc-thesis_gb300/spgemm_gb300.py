@@ -136,11 +136,15 @@ def library() -> C.CDLL:
         lib.spg_destroy.argtypes = [C.c_void_p]
         lib.spg_server_destroy.argtypes = [C.c_void_p]
         lib.spg_server_destroy.restype = None
+        lib.spg_plan_destroy.argtypes = [C.c_void_p]
+        lib.spg_plan_destroy.restype = None
+        lib.spg_plan_last_ms.argtypes = [C.c_void_p]
+        lib.spg_plan_last_ms.restype = C.c_float
         for name in ("spg_multiply", "spg_multiply_batch", "spg_accum_begin", "spg_accum_add", "spg_accum_finish",
                      "spg_result_download", "spg_result_free", "spg_scalar_multiplication_count",
                      "spg_scalar_multiplication_count_batch", "spg_last_timings", "spg_create", "spg_multiply_to_host",
                      "spg_config_default", "spg_server_create", "spg_submit", "spg_poll", "spg_cancel",
-                     "spg_server_result_free"):
+                     "spg_server_result_free", "spg_plan_create", "spg_plan_execute", "spg_plan_result"):
             getattr(lib, name).restype = C.c_int
         _lib = lib
     return _lib
@@ -299,6 +303,9 @@ class Engine:
         self._check(lib.spg_accum_end(self.h))
         return DeviceResult(self, res) if loc == SPG_DEVICE else _take_host(res, self)
 
+    def plan(self, pairs) -> "Plan":
+        return Plan(self, pairs)
+
     def scalar_multiplication_count_batch(self, pairs) -> list[int]:
         keep: list = []
         n = len(pairs)
@@ -319,6 +326,64 @@ class Engine:
         t = Timings()
         self._check(library().spg_last_timings(self.h, C.byref(t)))
         return t.as_dict()
+
+
+class Plan:
+    """spg_plan_*: the structure-dependent phases of n device-resident products
+    once, the value-dependent ones as a CUDA graph replayed by execute()."""
+
+    def __init__(self, engine: "Engine", pairs):
+        self._engine = engine
+        keep: list = []
+        n = len(pairs)
+        for a, b in pairs:
+            if not isinstance(a, DeviceCsr) or not isinstance(b, DeviceCsr):
+                raise TypeError("a plan needs DeviceCsr operands")
+        A = (_View * n)(*[_view(a, keep) for a, _ in pairs])
+        B = (_View * n)(*[_view(b, keep) for _, b in pairs])
+        p = C.c_void_p()
+        engine._check(library().spg_plan_create(engine.h, C.c_int32(n), A, B, C.byref(p)))
+        self.p, self.n, self._pairs = p, n, pairs
+
+    def execute(self) -> list[int]:
+        nnz = (C.c_int64 * self.n)()
+        self._engine._check(library().spg_plan_execute(self.p, nnz))
+        return [int(x) for x in nnz]
+
+    @property
+    def last_ms(self) -> float:
+        return float(library().spg_plan_last_ms(self.p))
+
+    def result(self, i: int) -> Csr:
+        """Host copy of product i of the last execution."""
+        res = _Result()
+        st = library().spg_plan_result(self.p, C.c_int32(i), C.byref(res))
+        if st != 0:
+            raise SpgError(st, "spg_plan_result failed (executed? index?)")
+        rp = np.empty(res.rows + 1, dtype=np.int64)
+        ci = np.empty(res.nnz, dtype=np.int32)
+        va = np.empty(res.nnz, dtype=np.float64)
+        self._engine._check(library().spg_result_download(
+            self._engine.h, C.byref(res), rp.ctypes.data_as(C.c_void_p),
+            ci.ctypes.data_as(C.c_void_p) if res.nnz else None, va.ctypes.data_as(C.c_void_p) if res.nnz else None))
+        return Csr(res.rows, res.cols, rp, ci, va)
+
+    def close(self):
+        if getattr(self, "p", None):
+            library().spg_plan_destroy(self.p)
+            self.p = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class _ServerConfig(C.Structure):
