@@ -304,6 +304,12 @@ def run_gpu_arm(args, rank, world, local):
     bytes_alg = sum(sg.algorithmic_bytes(a, b, sg.scalar_products_host(a, b), n)
                     for (a, b), n in zip(pairs, c_nnz))
 
+    # bin autotuner (untimed setup): per-bin team shape chosen by measured time on this workload
+    tuned = None
+    if not args.no_tune:
+        da, db = dev_pairs[0]
+        tuned = eng.tune(da, db, reps=2)
+
     stream = torch.cuda.ExternalStream(eng.stream, device=torch.device("cuda", local))
 
     def step():
@@ -431,7 +437,8 @@ def run_gpu_arm(args, rank, world, local):
                        "products_per_step": int(products), "c_nnz": int(sum(c_nnz)),
                        "l2": ("L2 flushed between timed steps (512 MiB write outside the events)" if flush
                               else f"inputs larger than L2 ({in_bytes / 1e6:.0f} MB, no flush)"),
-                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                       "bin_variants": tuned["variants"] if tuned else None},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(launches), "clocks": clocks.summary(), "graph_replay": replay,
             "phases_ms_last_step": {k: v for k, v in eng.last_timings().items()
@@ -683,6 +690,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-replay", action="store_true", help="skip the plan-replay (CUDA graph) sub-measurement")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default team shape in every bin")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -147,6 +147,25 @@ spg_status spg_scalar_multiplication_count(spg_handle* handle, const spg_csr_vie
 /* Per-phase timings of the last spg_multiply / spg_accum_add on the handle. */
 spg_status spg_last_timings(const spg_handle* handle, spg_timings* timings);
 
+/* ---- bin autotuner ----------------------------------------------------------------
+ * No reference counterpart.  Several numeric bins have two team shapes (warps
+ * per CTA x products per thread); results are identical, times differ with the
+ * workload.  spg_tune multiplies A * B reps times (after one warm-up) with every
+ * bin on its default shape, then on its alternative, and keeps, per bin, the
+ * alternative where its median numeric time was at least 3% lower.  The choice
+ * stays on the handle for later multiplies, batches, to-host products and plans
+ * (spg_get/set_bin_variants save and restore it: 20 entries of 0 or 1). */
+typedef struct {
+    float ms_bin[2][20];   /* median numeric time per bin: [0] default shapes, [1] alternatives */
+    int64_t bin_rows[20];
+    int64_t products;
+    uint8_t variant[20];   /* the choice now on the handle */
+} spg_tune_report;
+spg_status spg_tune(spg_handle* handle, const spg_csr_view* A, const spg_csr_view* B, int32_t reps,
+                    spg_tune_report* report);
+spg_status spg_get_bin_variants(const spg_handle* handle, uint8_t* variants);
+spg_status spg_set_bin_variants(spg_handle* handle, const uint8_t* variants);
+
 /* ---- accumulate mode -----------------------------------------------------
  * Replaces trident::LocalAccumulator (src/trident/common/matrix_blocks.hpp:23-32;
  * matrix_blocks.cpp:152-200): begin(rows, cols) <-> the constructor,

@@ -45,6 +45,8 @@ struct spg_handle {
     // page-locked staging for per-product reads of batches (grown on demand)
     void* host_scratch = nullptr;
     size_t host_scratch_bytes = 0;
+    // team shape of each numeric bin (0 default, 1 alternative), set by spg_tune
+    uint8_t bin_variant[kNumBins] = {};
 };
 
 namespace {
@@ -367,7 +369,7 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
     for (int b = 1; b < kNumBins; ++b) {
         if (!bin_count[b]) continue;
         launch_numeric(b, d_jobs, items + bin_off[b], bin_count[b], max_ub, scratch, scratch_bytes, &d_ctrl->stats,
-                       &d_ctrl->err, st, h->num_sms, !exact);
+                       &d_ctrl->err, st, h->num_sms, !exact, h->bin_variant[b]);
         cudaEventRecord(h->bin_ev[b], st);
     }
     check_cuda(cudaGetLastError(), "K4 launch");
@@ -808,6 +810,61 @@ spg_status spg_scalar_multiplication_count_batch(spg_handle* h, int32_t n, const
     });
 }
 
+spg_status spg_tune(spg_handle* h, const spg_csr_view* A, const spg_csr_view* B, int32_t reps,
+                    spg_tune_report* report) {
+    return guarded(h, [&] {
+        require(reps >= 1 && reps <= 64, SPG_INVALID_ARGUMENT, "reps must be in [1, 64]");
+        uint8_t saved[kNumBins];
+        std::memcpy(saved, h->bin_variant, sizeof saved);
+        spg_tune_report rep{};
+        try {
+            std::vector<JobIn> in{{A, B, CsrView{}}};
+            for (int v = 0; v < kNumVariants; ++v) {
+                std::memset(h->bin_variant, v, sizeof h->bin_variant);
+                std::vector<std::vector<float>> t(kNumBins);
+                for (int r = 0; r <= reps; ++r) {  // the first run warms up
+                    std::vector<DevResult> out;
+                    run_products(h, in, out, false, nullptr);
+                    for (auto& o : out) {
+                        cudaFreeAsync(o.rp, h->stream);
+                        cudaFreeAsync(o.ci, h->stream);
+                        cudaFreeAsync(o.v, h->stream);
+                    }
+                    if (r == 0) continue;
+                    for (int b = 0; b < kNumBins; ++b) t[b].push_back(h->last.ms_numeric_bin[b]);
+                }
+                for (int b = 0; b < kNumBins; ++b) {
+                    std::sort(t[b].begin(), t[b].end());
+                    rep.ms_bin[v][b] = t[b][t[b].size() / 2];
+                }
+                for (int b = 0; b < kNumBins; ++b) rep.bin_rows[b] = h->last.bin_rows[b];
+                rep.products = h->last.products;
+            }
+        } catch (...) {
+            std::memcpy(h->bin_variant, saved, sizeof saved);
+            throw;
+        }
+        for (int b = 0; b < kNumBins; ++b)  // the alternative only where it was measurably faster
+            rep.variant[b] = (rep.bin_rows[b] > 0 && rep.ms_bin[1][b] < 0.97f * rep.ms_bin[0][b]) ? 1 : 0;
+        std::memcpy(h->bin_variant, rep.variant, sizeof h->bin_variant);
+        if (report) *report = rep;
+    });
+}
+
+spg_status spg_get_bin_variants(const spg_handle* h, uint8_t* variants) {
+    if (!h || !variants) return SPG_INVALID_ARGUMENT;
+    std::memcpy(variants, h->bin_variant, kNumBins);
+    return SPG_OK;
+}
+
+spg_status spg_set_bin_variants(spg_handle* h, const uint8_t* variants) {
+    if (!h || !variants) return SPG_INVALID_ARGUMENT;
+    for (int b = 0; b < kNumBins; ++b)
+        if (variants[b] >= kNumVariants) return SPG_INVALID_ARGUMENT;
+    std::memcpy(h->bin_variant, variants, kNumBins);
+    return SPG_OK;
+}
+
 spg_status spg_last_timings(const spg_handle* h, spg_timings* t) {
     if (!h || !t) return SPG_INVALID_ARGUMENT;
     *t = h->last;
@@ -1053,7 +1110,7 @@ void plan_build(spg_plan* p, int32_t n, const spg_csr_view* A, const spg_csr_vie
     for (int b = 1; b < kNumBins; ++b)
         if (bin_count[b])
             launch_numeric(b, d_jobs, items + bin_off[b], bin_count[b], max_ub, scratch, scratch_bytes,
-                           &d_ctrl->stats, &d_ctrl->err, st, h->num_sms, true);
+                           &d_ctrl->stats, &d_ctrl->err, st, h->num_sms, true, h->bin_variant[b]);
     launch_scan(nz, static_cast<int64_t>(slots) - 1, partials, st);
     launch_compact_holes(d_jobs, n, d_row_base, total_rows, p->col, p->val, st);
     launch_gather(nz, d_idx, d_starts, n, st);

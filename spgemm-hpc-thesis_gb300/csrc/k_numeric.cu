@@ -399,8 +399,9 @@ size_t numeric_scratch_bytes(const int64_t* bin_count, int64_t max_ub, int num_s
 
 void launch_numeric(int bin, const Job* d_jobs, const int64_t* d_items, int64_t count, int64_t max_ub,
                     void* d_scratch, size_t, Stats* d_stats, ErrWord* d_err, cudaStream_t st, int num_sms,
-                    bool holes) {
+                    bool holes, int variant) {
     if (count <= 0) return;
+    if (variant == 1 && launch_numeric_alt(bin, d_jobs, d_items, count, d_stats, d_err, st, num_sms)) return;
     if (bin <= kLastWarpBin) {
         launch_numeric_warp(bin, d_jobs, d_items, count, d_stats, d_err, st, num_sms);
         return;

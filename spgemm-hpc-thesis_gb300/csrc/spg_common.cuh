@@ -189,9 +189,15 @@ size_t scan_partials_count(int64_t n);
 // K4: sorted, summed, zero-free rows into job.c_col/c_val and job.nz[row].
 // holes: upper-bound layout (rows above 16384 products are then split into
 // column-range pieces; in the exact layout they keep the global-slab sort).
+// variant: 0 the default team shape of the bin, 1 its alternative (where the
+// bin has one; see launch_numeric_alt).
 void launch_numeric(int bin, const Job* d_jobs, const int64_t* d_items, int64_t count, int64_t max_ub,
                     void* d_scratch, size_t scratch_bytes, Stats* d_stats, ErrWord* d_err,
-                    cudaStream_t stream, int num_sms, bool holes);
+                    cudaStream_t stream, int num_sms, bool holes, int variant = 0);
+// The alternative shape of a bin; false if the bin has none.
+bool launch_numeric_alt(int bin, const Job* d_jobs, const int64_t* d_items, int64_t count, Stats* d_stats,
+                        ErrWord* d_err, cudaStream_t stream, int num_sms);
+constexpr int kNumVariants = 2;
 // K4 for the warp-per-row bins (1..kLastWarpBin), compiled separately.
 void launch_numeric_warp(int bin, const Job* d_jobs, const int64_t* d_items, int64_t count, Stats* d_stats,
                          ErrWord* d_err, cudaStream_t stream, int num_sms);

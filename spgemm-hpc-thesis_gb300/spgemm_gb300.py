@@ -110,6 +110,19 @@ class Timings(C.Structure):
         return d
 
 
+class TuneReport(C.Structure):
+    _fields_ = [("ms_bin", (C.c_float * 20) * 2), ("bin_rows", C.c_int64 * 20), ("products", C.c_int64),
+                ("variant", C.c_uint8 * 20)]
+
+    def as_dict(self) -> dict:
+        bins = {}
+        for i, name in enumerate(BIN_NAMES):
+            if self.bin_rows[i]:
+                bins[name] = {"ms_default": round(self.ms_bin[0][i], 4), "ms_alt": round(self.ms_bin[1][i], 4),
+                              "variant": int(self.variant[i])}
+        return {"products": int(self.products), "bins": bins, "variants": list(self.variant)}
+
+
 class _SynthCsr(C.Structure):
     _fields_ = [("rows", C.c_int32), ("cols", C.c_int32), ("nnz", C.c_int64),
                 ("row_ptr", C.POINTER(C.c_int64)), ("col", C.POINTER(C.c_int32)), ("val", C.POINTER(C.c_double))]
@@ -144,7 +157,8 @@ def library() -> C.CDLL:
                      "spg_result_download", "spg_result_free", "spg_scalar_multiplication_count",
                      "spg_scalar_multiplication_count_batch", "spg_last_timings", "spg_create", "spg_multiply_to_host",
                      "spg_config_default", "spg_server_create", "spg_submit", "spg_poll", "spg_cancel",
-                     "spg_server_result_free", "spg_plan_create", "spg_plan_execute", "spg_plan_result"):
+                     "spg_server_result_free", "spg_plan_create", "spg_plan_execute", "spg_plan_result", "spg_tune",
+                     "spg_get_bin_variants", "spg_set_bin_variants"):
             getattr(lib, name).restype = C.c_int
         _lib = lib
     return _lib
@@ -302,6 +316,25 @@ class Engine:
         self._check(lib.spg_accum_finish(self.h, C.c_int32(loc), C.byref(res)))
         self._check(lib.spg_accum_end(self.h))
         return DeviceResult(self, res) if loc == SPG_DEVICE else _take_host(res, self)
+
+    def tune(self, a, b, reps: int = 3) -> dict:
+        """spg_tune: per-bin choice between the default and the alternative team shape."""
+        keep: list = []
+        va, vb = _view(a, keep), _view(b, keep)
+        rep = TuneReport()
+        self._check(library().spg_tune(self.h, C.byref(va), C.byref(vb), C.c_int32(reps), C.byref(rep)))
+        return rep.as_dict()
+
+    @property
+    def bin_variants(self) -> list[int]:
+        v = (C.c_uint8 * 20)()
+        self._check(library().spg_get_bin_variants(self.h, v))
+        return list(v)
+
+    @bin_variants.setter
+    def bin_variants(self, values) -> None:
+        v = (C.c_uint8 * 20)(*values)
+        self._check(library().spg_set_bin_variants(self.h, v))
 
     def plan(self, pairs) -> "Plan":
         return Plan(self, pairs)
