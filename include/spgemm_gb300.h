@@ -197,6 +197,32 @@ spg_status spg_multiply_batch(spg_handle* handle, int32_t n, const spg_csr_view*
 spg_status spg_scalar_multiplication_count_batch(spg_handle* handle, int32_t n, const spg_csr_view* A,
                                                  const spg_csr_view* B, int64_t* products);
 
+/* ---- validation (the reference's Full and Partial modes, on the GPU) -------------
+ * Replaces validateProduct(A, B, C, ValidationMode::Full / Partial)
+ * (src/common/spgemm_common.cpp:720-851 validateFullStreaming, :541-572
+ * buildPartialReference / comparePartialReference) without their caches.  Every
+ * coordinate of A * B is recomputed by the reference's own algorithm -- one
+ * thread per row walks the row's products in stored order into its own hash
+ * table -- as the sequential FP64 sum, a double-double sum of the exact
+ * products (the reference uses long double), the double-double magnitude sum
+ * and the term count; C is then merged against it.  `passed` (Full): every
+ * walked coordinate satisfies the roundoff bound of coordinateBound (:663-675)
+ * evaluated with upward rounding (reference precision 2^-100 in place of long
+ * double's).  `partial_passed` (Partial): C's row counts equal the counts of
+ * nonzero sequential sums.  Malformed or non-finite operands give
+ * matrices_ok = 0 and passed = 0, as in the reference.  median_rel_error is the
+ * midpoint of a histogram bucket (relative resolution 1/16).  The call returns
+ * SPG_OK whenever the check ran, whatever its verdict. */
+typedef struct {
+    int32_t passed, environment_ok, matrices_ok, partial_passed;
+    int64_t rejected, row_nnz_mismatches, support_mismatches, reference_nnz, checked_coordinates;
+    double max_abs_error;     /* max |c - sequential FP64 sum| */
+    double max_error_ratio;   /* max |c - reference| / bound (capped at 1 where accepted) */
+    double max_rel_error, median_rel_error;  /* over stored coordinates, against the reference sum */
+} spg_full_report;
+spg_status spg_validate_full(spg_handle* handle, const spg_csr_view* A, const spg_csr_view* B, const spg_csr_view* C,
+                             spg_full_report* report);
+
 /* ---- plans: one sparsity structure, many value sets ------------------------------
  * No reference counterpart.  For products whose operands keep their structure
  * (row offsets and columns) while their values change -- a Galerkin product

@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <limits>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -848,6 +849,104 @@ spg_status spg_tune(spg_handle* h, const spg_csr_view* A, const spg_csr_view* B,
             rep.variant[b] = (rep.bin_rows[b] > 0 && rep.ms_bin[1][b] < 0.97f * rep.ms_bin[0][b]) ? 1 : 0;
         std::memcpy(h->bin_variant, rep.variant, sizeof h->bin_variant);
         if (report) *report = rep;
+    });
+}
+
+spg_status spg_validate_full(spg_handle* h, const spg_csr_view* A, const spg_csr_view* B, const spg_csr_view* C,
+                             spg_full_report* rep) {
+    return guarded(h, [&] {
+        require(A && B && C && rep, SPG_INVALID_ARGUMENT, "bad validation arguments");
+        check_view(A, "A");
+        check_view(B, "B");
+        check_view(C, "C");
+        std::memset(rep, 0, sizeof(*rep));
+        rep->environment_ok = 1;  // IEEE FP64, round to nearest, gradual underflow on the device
+        rep->max_abs_error = std::numeric_limits<double>::infinity();
+        rep->rejected = 1;
+        cudaStream_t st = h->stream;
+        Arena ar(h);
+        const CsrView a = stage(h, ar, A);
+        const CsrView b = stage(h, ar, B);
+        const CsrView c = stage(h, ar, C);
+        int* d_flag = ar.alloc<int>(1, "flag");
+        check_cuda(cudaMemsetAsync(d_flag, 0, sizeof(int), st), "memset");
+        const bool shapes = A->cols == B->rows && C->rows == A->rows && C->cols == B->cols;
+        launch_validate_csr(a, false, d_flag, st);
+        launch_validate_csr(b, false, d_flag, st);
+        launch_validate_csr(c, true, d_flag, st);
+        int* h_flag = static_cast<int*>(host_staging(h, 64));
+        launch_readback(d_flag, h_flag, 8, st);  // flag plus padding (allocations are >= 16 bytes)
+        sync(h);
+        rep->matrices_ok = shapes && h_flag[0] == 0;
+        if (!rep->matrices_ok) return;
+        const int32_t m = A->rows;
+        int64_t* slot_off = ar.alloc<int64_t>(static_cast<size_t>(m) + 1, "slots");
+        int64_t* partials = ar.alloc<int64_t>(scan_partials_count(static_cast<int64_t>(m) + 1), "partials");
+        check_cuda(cudaMemsetAsync(slot_off, 0, sizeof(int64_t) * (static_cast<size_t>(m) + 1), st), "memset");
+        launch_validate_slots(a, b, slot_off, st);
+        launch_scan(slot_off, m, partials, st);
+        std::vector<int64_t> off(static_cast<size_t>(m) + 1);
+        int64_t* h_off = static_cast<int64_t*>(host_staging(h, sizeof(int64_t) * (static_cast<size_t>(m) + 1)));
+        launch_readback(slot_off, h_off, sizeof(int64_t) * (static_cast<size_t>(m) + 1), st);
+        const int nb = validate_hist_buckets();
+        unsigned long long* d_counters = ar.alloc<unsigned long long>(8, "counters");
+        double* d_maxima = ar.alloc<double>(4, "maxima");
+        unsigned long long* d_hist = ar.alloc<unsigned long long>(static_cast<size_t>(nb), "histogram");
+        check_cuda(cudaMemsetAsync(d_counters, 0, 8 * sizeof(unsigned long long), st), "memset");
+        check_cuda(cudaMemsetAsync(d_maxima, 0, 4 * sizeof(double), st), "memset");
+        check_cuda(cudaMemsetAsync(d_hist, 0, sizeof(unsigned long long) * nb, st), "memset");
+        sync(h);
+        std::copy(h_off, h_off + m + 1, off.begin());
+        // row chunks whose tables fit kChunkCells cells (a bigger row alone gets its own)
+        constexpr int64_t kChunkCells = int64_t{1} << 27;
+        int64_t max_chunk = 0;
+        std::vector<int32_t> cuts{0};
+        for (int32_t r = 0; r < m;) {
+            int32_t e = r + 1;
+            while (e < m && off[e + 1] - off[r] <= kChunkCells) ++e;
+            max_chunk = std::max(max_chunk, off[e] - off[r]);
+            cuts.push_back(e);
+            r = e;
+        }
+        void* table = ar.alloc<unsigned char>(static_cast<size_t>(max_chunk) * validate_cell_bytes(), "cell tables");
+        for (size_t i = 0; i + 1 < cuts.size(); ++i)
+            launch_validate_rows(a, b, c, cuts[i], cuts[i + 1], slot_off, table, d_counters, d_maxima, d_hist, st);
+        check_cuda(cudaGetLastError(), "validation launch");
+        const size_t back = 8 * sizeof(unsigned long long) + 4 * sizeof(double) + sizeof(unsigned long long) * nb;
+        unsigned char* hb = static_cast<unsigned char*>(host_staging(h, back));
+        launch_readback(d_counters, hb, 8 * sizeof(unsigned long long), st);
+        launch_readback(d_maxima, hb + 64, 4 * sizeof(double), st);
+        launch_readback(d_hist, hb + 96, sizeof(unsigned long long) * nb, st);
+        sync(h);
+        const unsigned long long* cnt = reinterpret_cast<const unsigned long long*>(hb);
+        const double* mx = reinterpret_cast<const double*>(hb + 64);
+        const unsigned long long* hist = reinterpret_cast<const unsigned long long*>(hb + 96);
+        rep->rejected = static_cast<int64_t>(cnt[0]);
+        rep->row_nnz_mismatches = static_cast<int64_t>(cnt[1]);
+        rep->support_mismatches = static_cast<int64_t>(cnt[2]);
+        rep->reference_nnz = static_cast<int64_t>(cnt[3]);
+        rep->checked_coordinates = static_cast<int64_t>(cnt[4]);
+        rep->max_abs_error = mx[0];
+        rep->max_error_ratio = mx[1];
+        rep->max_rel_error = mx[2];
+        unsigned long long total = 0;
+        for (int i = 0; i < nb; ++i) total += hist[i];
+        if (total) {
+            unsigned long long seen = 0;
+            int i = 0;
+            for (; i < nb; ++i) {
+                seen += hist[i];
+                if (seen > total / 2) break;
+            }
+            // bucket i holds the doubles whose top 14 bits are i: report its midpoint
+            uint64_t lo_bits = static_cast<uint64_t>(i) << 49, hi_bits = (static_cast<uint64_t>(i) + 1) << 49;
+            double lo, hi;
+            std::memcpy(&lo, &lo_bits, 8);
+            std::memcpy(&hi, &hi_bits, 8);
+            rep->median_rel_error = 0.5 * (lo + hi);
+        }
+        rep->passed = rep->rejected == 0;
+        rep->partial_passed = rep->row_nnz_mismatches == 0;
     });
 }
 

@@ -220,6 +220,14 @@ struct RebaseItem {
 };
 void launch_gather(const int64_t* d_src, const int64_t* d_idx, int64_t* d_dst, int n, cudaStream_t stream);
 void launch_rebase(const RebaseItem* d_items, int n, int64_t max_rows, cudaStream_t stream);
+// GPU validator (k_validate.cu).
+size_t validate_cell_bytes();
+int validate_hist_buckets();
+void launch_validate_csr(const CsrView& M, bool ordered, int* d_flag, cudaStream_t st);
+void launch_validate_slots(const CsrView& A, const CsrView& B, int64_t* d_slots, cudaStream_t st);
+void launch_validate_rows(const CsrView& A, const CsrView& B, const CsrView& C, int32_t row0, int32_t row1,
+                          const int64_t* d_slot_off, void* d_table, unsigned long long* d_counters,
+                          double* d_maxima, unsigned long long* d_hist, cudaStream_t st);
 // Copies `bytes` (a multiple of 8, 8-byte aligned) from device memory into
 // page-locked host memory with a kernel (no copy engine involved).
 void launch_readback(const void* d_src, void* h_dst, size_t bytes, cudaStream_t stream);

@@ -110,6 +110,17 @@ class Timings(C.Structure):
         return d
 
 
+class FullReport(C.Structure):
+    _fields_ = [("passed", C.c_int32), ("environment_ok", C.c_int32), ("matrices_ok", C.c_int32),
+                ("partial_passed", C.c_int32), ("rejected", C.c_int64), ("row_nnz_mismatches", C.c_int64),
+                ("support_mismatches", C.c_int64), ("reference_nnz", C.c_int64),
+                ("checked_coordinates", C.c_int64), ("max_abs_error", C.c_double),
+                ("max_error_ratio", C.c_double), ("max_rel_error", C.c_double), ("median_rel_error", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 class TuneReport(C.Structure):
     _fields_ = [("ms_bin", (C.c_float * 20) * 2), ("bin_rows", C.c_int64 * 20), ("products", C.c_int64),
                 ("variant", C.c_uint8 * 20)]
@@ -158,7 +169,7 @@ def library() -> C.CDLL:
                      "spg_scalar_multiplication_count_batch", "spg_last_timings", "spg_create", "spg_multiply_to_host",
                      "spg_config_default", "spg_server_create", "spg_submit", "spg_poll", "spg_cancel",
                      "spg_server_result_free", "spg_plan_create", "spg_plan_execute", "spg_plan_result", "spg_tune",
-                     "spg_get_bin_variants", "spg_set_bin_variants"):
+                     "spg_get_bin_variants", "spg_set_bin_variants", "spg_validate_full"):
             getattr(lib, name).restype = C.c_int
         _lib = lib
     return _lib
@@ -316,6 +327,18 @@ class Engine:
         self._check(lib.spg_accum_finish(self.h, C.c_int32(loc), C.byref(res)))
         self._check(lib.spg_accum_end(self.h))
         return DeviceResult(self, res) if loc == SPG_DEVICE else _take_host(res, self)
+
+    def validate_full(self, a, b, c) -> dict:
+        """spg_validate_full: the reference's Full and Partial checks of C against A * B, on the GPU."""
+        keep: list = []
+        va, vb = _view(a, keep), _view(b, keep)
+        if isinstance(c, DeviceResult):
+            vc = _View(c.rows, c.cols, c.nnz, c._res.row_ptr, c._res.col, c._res.val, SPG_DEVICE)
+        else:
+            vc = _view(c, keep)
+        rep = FullReport()
+        self._check(library().spg_validate_full(self.h, C.byref(va), C.byref(vb), C.byref(vc), C.byref(rep)))
+        return rep.as_dict()
 
     def tune(self, a, b, reps: int = 3) -> dict:
         """spg_tune: per-bin choice between the default and the alternative team shape."""
