@@ -38,7 +38,8 @@ typedef enum {
     SPG_DEVICE_TIMEOUT = 6,        /* a bounded wait ran out (serving loop) */
     SPG_CUDA_ERROR = 7,            /* any other CUDA failure */
     SPG_NOT_READY = 8,             /* spg_poll: the request has not finished */
-    SPG_CANCELLED = 9              /* spg_poll: the request was cancelled */
+    SPG_CANCELLED = 9,             /* spg_poll: the request was cancelled */
+    SPG_FORMAT_ERROR = 10          /* spg_read_matrix_market: unreadable or malformed file (std::runtime_error) */
 } spg_status;
 
 typedef enum { SPG_HOST = 0, SPG_DEVICE = 1 } spg_location;
@@ -196,6 +197,30 @@ spg_status spg_multiply_batch(spg_handle* handle, int32_t n, const spg_csr_view*
  * products[i] = P of A[i] * B[i]; errors as spg_scalar_multiplication_count. */
 spg_status spg_scalar_multiplication_count_batch(spg_handle* handle, int32_t n, const spg_csr_view* A,
                                                  const spg_csr_view* B, int64_t* products);
+
+/* ---- Matrix Market input and transposition ----------------------------------------
+ * spg_read_matrix_market replaces CsrMatrix readMatrixMarket(const std::string&)
+ * (src/common/matrix_market.hpp; matrix_market.cpp:28-145) with the same
+ * semantics: coordinate real / integer / pattern matrices, general / symmetric /
+ * skew-symmetric / hermitian storage (mirrored entries appended after their
+ * entry, negated for skew-symmetric), comments and empty lines skipped, 'D'
+ * exponents accepted, entries kept in file order with duplicates, rows built by
+ * a stable counting sort.  The entry lines are parsed on all host threads.  The
+ * reference's std::runtime_error cases return SPG_FORMAT_ERROR with the message
+ * in err (err_len bytes, may be NULL).  The result is in host (malloc) or
+ * device memory; release it with spg_result_free on any handle (or
+ * spg_csr_release without one). */
+spg_status spg_read_matrix_market(const char* path, int32_t out_location, spg_csr_result* C, char* err,
+                                  size_t err_len);
+/* Frees a result without a handle (host results, or device results when no
+ * stream ordering is needed: the device arrays are freed synchronously). */
+void spg_csr_release(spg_csr_result* C);
+/* C = A^T on the device: C's row j holds A's column j in A's row-major order
+ * (the order of a stable sort by column; Gustavson's permuted transposition,
+ * the classical companion of the row-wise product the reference cites in
+ * docs/sources.md).  No reference counterpart: it forms R^T of the Galerkin
+ * chain R A R^T on the device. */
+spg_status spg_transpose(spg_handle* handle, const spg_csr_view* A, int32_t out_location, spg_csr_result* C);
 
 /* ---- validation (the reference's Full and Partial modes, on the GPU) -------------
  * Replaces validateProduct(A, B, C, ValidationMode::Full / Partial)

@@ -21,7 +21,7 @@ CSRC = HERE / "csrc"
 OBJ = HERE / "_build" / platform.machine()  # host objects differ per architecture
 LIB = HERE / "libspgemm_gb300.so"
 SOURCES = ["engine.cu", "k_rowwork.cu", "k_symbolic.cu", "k_numeric.cu", "k_numeric_warp.cu", "k_numeric_alt.cu",
-           "k_validate.cu", "noalloc.cu", "server.cu"]
+           "k_validate.cu", "k_transpose.cu", "mtx.cu", "noalloc.cu", "server.cu"]
 HEADERS = ["spg_common.cuh", "spg_enum.cuh", "k_numeric_row.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-O3",

@@ -631,6 +631,7 @@ const char* spg_status_string(spg_status s) {
         case SPG_CUDA_ERROR: return "SPG_CUDA_ERROR";
         case SPG_NOT_READY: return "SPG_NOT_READY";
         case SPG_CANCELLED: return "SPG_CANCELLED";
+        case SPG_FORMAT_ERROR: return "SPG_FORMAT_ERROR";
     }
     return "unknown spg_status";
 }
@@ -947,6 +948,38 @@ spg_status spg_validate_full(spg_handle* h, const spg_csr_view* A, const spg_csr
         }
         rep->passed = rep->rejected == 0;
         rep->partial_passed = rep->row_nnz_mismatches == 0;
+    });
+}
+
+spg_status spg_transpose(spg_handle* h, const spg_csr_view* A, int32_t out_location, spg_csr_result* C) {
+    return guarded(h, [&] {
+        require(C != nullptr, SPG_INVALID_ARGUMENT, "C is NULL");
+        require(out_location == SPG_HOST || out_location == SPG_DEVICE, SPG_INVALID_ARGUMENT, "bad out_location");
+        check_view(A, "A");
+        cudaStream_t st = h->stream;
+        Arena ar(h);
+        const CsrView a = stage(h, ar, A);
+        int* d_flag = ar.alloc<int>(1, "flag");
+        check_cuda(cudaMemsetAsync(d_flag, 0, sizeof(int), st), "memset");
+        launch_validate_csr(a, false, d_flag, st, false);
+        int* h_flag = static_cast<int*>(host_staging(h, 64));
+        launch_readback(d_flag, h_flag, 8, st);
+        sync(h);
+        require(h_flag[0] == 0, SPG_INVALID_ARGUMENT, "malformed CSR operand (offsets or columns out of range)");
+        DevResult r;
+        r.rows = A->cols;
+        r.cols = A->rows;
+        r.nnz = A->nnz;
+        r.rp = ar.alloc<int64_t>(static_cast<size_t>(A->cols) + 1, "transpose row_ptr");
+        r.ci = ar.alloc<int32_t>(static_cast<size_t>(A->nnz), "transpose col");
+        r.v = ar.alloc<double>(static_cast<size_t>(A->nnz), "transpose val");
+        void* scratch = ar.alloc<unsigned char>(transpose_scratch_bytes(A->nnz, A->cols), "transpose scratch");
+        launch_transpose(a.rp, a.ci, a.v, A->rows, A->cols, A->nnz, r.rp, r.ci, r.v, scratch, st);
+        check_cuda(cudaGetLastError(), "transpose launch");
+        ar.release(r.rp);
+        ar.release(r.ci);
+        ar.release(r.v);
+        deliver(h, r, out_location, C);
     });
 }
 

@@ -227,7 +227,7 @@ __global__ void validate_slots_kernel(CsrView A, CsrView B, int64_t* __restrict_
 // validNumericCsr (spgemm_common.cpp:621-638): offsets, column range, finite
 // values, and (ordered) strictly increasing columns per row.  flag[0] = 1 on
 // any violation.
-__global__ void validate_csr_kernel(CsrView M, int ordered, int* __restrict__ flag) {
+__global__ void validate_csr_kernel(CsrView M, int ordered, int finite, int* __restrict__ flag) {
     for (int32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < M.rows; r += gridDim.x * blockDim.x) {
         const int64_t first = M.rp[r], end = M.rp[r + 1];
         if ((r == 0 && first != 0) || (r == M.rows - 1 && end != M.nnz) || first < 0 || end < first || end > M.nnz) {
@@ -237,7 +237,7 @@ __global__ void validate_csr_kernel(CsrView M, int ordered, int* __restrict__ fl
         int32_t prev = -1;
         for (int64_t p = first; p < end; ++p) {
             const int32_t c = M.ci[p];
-            if (c < 0 || c >= M.cols || (ordered && c <= prev) || !isfinite(M.v[p])) {
+            if (c < 0 || c >= M.cols || (ordered && c <= prev) || (finite && !isfinite(M.v[p]))) {
                 *flag = 1;
                 break;
             }
@@ -256,9 +256,9 @@ int grid_rows(int64_t rows, int threads) {
 size_t validate_cell_bytes() { return sizeof(Cell); }
 int validate_hist_buckets() { return kHistBuckets; }
 
-void launch_validate_csr(const CsrView& M, bool ordered, int* d_flag, cudaStream_t st) {
+void launch_validate_csr(const CsrView& M, bool ordered, int* d_flag, cudaStream_t st, bool finite) {
     if (M.rows <= 0) return;
-    validate_csr_kernel<<<grid_rows(M.rows, 128), 128, 0, st>>>(M, ordered ? 1 : 0, d_flag);
+    validate_csr_kernel<<<grid_rows(M.rows, 128), 128, 0, st>>>(M, ordered ? 1 : 0, finite ? 1 : 0, d_flag);
 }
 
 void launch_validate_slots(const CsrView& A, const CsrView& B, int64_t* d_slots, cudaStream_t st) {

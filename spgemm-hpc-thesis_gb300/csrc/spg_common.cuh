@@ -223,7 +223,13 @@ void launch_rebase(const RebaseItem* d_items, int n, int64_t max_rows, cudaStrea
 // GPU validator (k_validate.cu).
 size_t validate_cell_bytes();
 int validate_hist_buckets();
-void launch_validate_csr(const CsrView& M, bool ordered, int* d_flag, cudaStream_t st);
+// flag[0] = 1 if M is malformed (offsets, column range, ordered: strictly
+// increasing columns, finite: finite values).
+void launch_validate_csr(const CsrView& M, bool ordered, int* d_flag, cudaStream_t st, bool finite = true);
+// CSR transpose (k_transpose.cu): A^T's rows keep A's row-major order.
+size_t transpose_scratch_bytes(int64_t nnz, int32_t cols);
+void launch_transpose(const int64_t* rp, const int32_t* col, const double* val, int32_t rows, int32_t cols, int64_t nnz,
+                      int64_t* out_rp, int32_t* out_col, double* out_val, void* scratch, cudaStream_t st);
 void launch_validate_slots(const CsrView& A, const CsrView& B, int64_t* d_slots, cudaStream_t st);
 void launch_validate_rows(const CsrView& A, const CsrView& B, const CsrView& C, int32_t row0, int32_t row1,
                           const int64_t* d_slot_off, void* d_table, unsigned long long* d_counters,

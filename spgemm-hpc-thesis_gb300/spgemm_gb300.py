@@ -26,7 +26,7 @@ SYNTH_PATH = HERE / "libspg_synth.so"
 SPG_HOST, SPG_DEVICE = 0, 1
 STATUS_NAMES = {0: "SPG_OK", 1: "SPG_INVALID_ARGUMENT", 2: "SPG_OVERFLOW", 3: "SPG_OUT_OF_RANGE_COLUMN",
                 4: "SPG_OUT_OF_MEMORY", 5: "SPG_BUDGET_EXCEEDED", 6: "SPG_DEVICE_TIMEOUT", 7: "SPG_CUDA_ERROR",
-                8: "SPG_NOT_READY", 9: "SPG_CANCELLED"}
+                8: "SPG_NOT_READY", 9: "SPG_CANCELLED", 10: "SPG_FORMAT_ERROR"}
 BIN_NAMES = ["empty", "w<=32", "w<=64", "w<=96", "w<=128", "w<=192", "w<=256", "w<=384", "w<=512", "b<=768",
              "b<=1K", "b<=1.5K", "b<=2K", "b<=3K", "b<=4K", "b<=6K", "b<=8K", "b<=12K", "b<=16K", "heavy"]
 
@@ -160,6 +160,8 @@ def library() -> C.CDLL:
         lib.spg_destroy.argtypes = [C.c_void_p]
         lib.spg_server_destroy.argtypes = [C.c_void_p]
         lib.spg_server_destroy.restype = None
+        lib.spg_csr_release.argtypes = [C.c_void_p]
+        lib.spg_csr_release.restype = None
         lib.spg_plan_destroy.argtypes = [C.c_void_p]
         lib.spg_plan_destroy.restype = None
         lib.spg_plan_last_ms.argtypes = [C.c_void_p]
@@ -169,7 +171,8 @@ def library() -> C.CDLL:
                      "spg_scalar_multiplication_count_batch", "spg_last_timings", "spg_create", "spg_multiply_to_host",
                      "spg_config_default", "spg_server_create", "spg_submit", "spg_poll", "spg_cancel",
                      "spg_server_result_free", "spg_plan_create", "spg_plan_execute", "spg_plan_result", "spg_tune",
-                     "spg_get_bin_variants", "spg_set_bin_variants", "spg_validate_full"):
+                     "spg_get_bin_variants", "spg_set_bin_variants", "spg_validate_full", "spg_transpose",
+                     "spg_read_matrix_market"):
             getattr(lib, name).restype = C.c_int
         _lib = lib
     return _lib
@@ -328,6 +331,15 @@ class Engine:
         self._check(lib.spg_accum_end(self.h))
         return DeviceResult(self, res) if loc == SPG_DEVICE else _take_host(res, self)
 
+    def transpose(self, a, out: str = "host"):
+        """spg_transpose: A^T with every row in A's row-major order."""
+        keep: list = []
+        va = _view(a, keep)
+        res = _Result()
+        loc = SPG_DEVICE if out == "device" else SPG_HOST
+        self._check(library().spg_transpose(self.h, C.byref(va), C.c_int32(loc), C.byref(res)))
+        return DeviceResult(self, res) if loc == SPG_DEVICE else _take_host(res, self)
+
     def validate_full(self, a, b, c) -> dict:
         """spg_validate_full: the reference's Full and Partial checks of C against A * B, on the GPU."""
         keep: list = []
@@ -440,6 +452,41 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+def read_matrix_market(path, out: str = "host"):
+    """spg_read_matrix_market: the reference's readMatrixMarket semantics
+    (matrix_market.cpp:28-145).  out="host" returns a Csr; out="device" a
+    DeviceCsr (torch tensors holding a copy of the library's device arrays)."""
+    lib = library()
+    res = _Result()
+    err = C.create_string_buffer(256)
+    loc = SPG_DEVICE if out == "device" else SPG_HOST
+    st = lib.spg_read_matrix_market(str(path).encode(), C.c_int32(loc), C.byref(res), err, C.c_size_t(256))
+    if st != 0:
+        raise SpgError(st, err.value.decode(errors="replace"))
+    try:
+        if loc == SPG_HOST:
+            rows, nnz = res.rows, res.nnz
+            rp = np.ctypeslib.as_array(C.cast(res.row_ptr, C.POINTER(C.c_int64)), shape=(rows + 1,)).copy()
+            ci = (np.ctypeslib.as_array(C.cast(res.col, C.POINTER(C.c_int32)), shape=(nnz,)).copy() if nnz
+                  else np.zeros(0, np.int32))
+            va = (np.ctypeslib.as_array(C.cast(res.val, C.POINTER(C.c_double)), shape=(nnz,)).copy() if nnz
+                  else np.zeros(0, np.float64))
+            return Csr(rows, res.cols, rp, ci, va)
+        import torch
+        dev = torch.device("cuda", torch.cuda.current_device())
+        rp = torch.empty(res.rows + 1, dtype=torch.int64, device=dev)
+        ci = torch.empty(max(res.nnz, 1), dtype=torch.int32, device=dev)
+        va = torch.empty(max(res.nnz, 1), dtype=torch.float64, device=dev)
+        torch.cuda.synchronize()
+        cudart = C.CDLL("libcudart.so")
+        for dst, src, nb in ((rp, res.row_ptr, 8 * (res.rows + 1)), (ci, res.col, 4 * res.nnz), (va, res.val, 8 * res.nnz)):
+            if nb and cudart.cudaMemcpy(C.c_void_p(dst.data_ptr()), C.c_void_p(src), C.c_size_t(nb), 3) != 0:
+                raise SpgError(7, "device copy failed")
+        return DeviceCsr(res.rows, res.cols, rp, ci[:res.nnz], va[:res.nnz])
+    finally:
+        lib.spg_csr_release(C.byref(res))
 
 
 class _ServerConfig(C.Structure):

@@ -48,7 +48,11 @@ def test_validation_verdicts(port, name):
     full = port.validate_full(a, b, c)
     assert bool(full["passed"]) == meta["full_passed"]
     if meta["full_passed"]:
-        assert full["max_error_ratio"] == pytest.approx(meta["full_max_error_ratio"], rel=0, abs=0)
+        # The golden ratios come from the reference built where long double is the
+        # x87 80-bit format; where long double has another precision (aarch64:
+        # 128-bit) the reference sum, and so the ratio, differs in late digits.
+        tol = 0 if np.finfo(np.longdouble).nmant == 63 else 1e-3
+        assert full["max_error_ratio"] == pytest.approx(meta["full_max_error_ratio"], rel=tol, abs=0)
 
 
 @pytest.mark.parametrize("name", ACCUMS)
