@@ -7,8 +7,8 @@
 //   std::vector<double> values.
 // Statuses become the reference's exception types: std::invalid_argument for
 // shapes and malformed input, std::overflow_error for counts, std::runtime_error
-// for an A column outside B's rows (spgemm_common.cpp:141-143), std::bad_alloc
-// for device memory.
+// for an A column outside B's rows (spgemm_common.cpp:141-143) and for a
+// malformed Matrix Market file, std::bad_alloc for device memory.
 #pragma once
 
 #include <cstdint>
@@ -119,6 +119,44 @@ inline Engine& thread_engine() {
 template <class Csr>
 Csr spgemm(const Csr& a, const Csr& b) {
     return thread_engine().multiply(a, b);
+}
+
+// Drop-in for readMatrixMarket(path) (matrix_market.hpp; matrix_market.cpp:28-145):
+// the same CsrMatrix, std::runtime_error for the same malformed files.
+template <class Csr>
+Csr readMatrixMarket(const std::string& path) {
+    spg_csr_result r;
+    char err[256] = {0};
+    const spg_status s = spg_read_matrix_market(path.c_str(), SPG_HOST, &r, err, sizeof err);
+    if (s != SPG_OK) throw_status(s, err);
+    Csr out;
+    out.rows = r.rows;
+    out.cols = r.cols;
+    out.rowPtr.assign(r.row_ptr, r.row_ptr + r.rows + 1);
+    out.columnIndices.assign(r.col, r.col + r.nnz);
+    out.values.assign(r.val, r.val + r.nnz);
+    spg_csr_release(&r);
+    return out;
+}
+
+// The reference's Full-mode verdict of validateProduct(A, B, C, ValidationMode::Full)
+// (spgemm_common.cpp:720-851), computed on the GPU (the report also holds the
+// Partial verdict of comparePartialReference, :541-572).
+template <class Csr>
+spg_full_report validateFull(const Csr& a, const Csr& b, const Csr& c, Engine& engine = thread_engine()) {
+    const spg_csr_view va = host_view(a), vb = host_view(b), vc = host_view(c);
+    spg_full_report rep;
+    engine.check(spg_validate_full(engine.handle(), &va, &vb, &vc, &rep));
+    return rep;
+}
+
+// A^T with every row in A's row-major order.
+template <class Csr>
+Csr transpose(const Csr& a, Engine& engine = thread_engine()) {
+    const spg_csr_view va = host_view(a);
+    spg_csr_result r;
+    engine.check(spg_transpose(engine.handle(), &va, SPG_DEVICE, &r));
+    return engine.template download<Csr>(r);
 }
 
 // Drop-in for trident::LocalAccumulator (matrix_blocks.hpp:23-32).  One

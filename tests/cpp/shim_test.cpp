@@ -83,6 +83,36 @@ int main() {
         g::LocalAccumulator<CsrMatrix> empty(0, 4);
         REQUIRE(empty.finish().rowPtr == std::vector<int64_t>{0});
     }
+    // the reference's validation, its Matrix Market reader and a transposition, through the same layer
+    {
+        const spg_full_report rep = g::validateFull(ca, cb, cc);
+        REQUIRE(rep.passed == 1 && rep.partial_passed == 1 && rep.matrices_ok == 1 && rep.rejected == 0);
+        CsrMatrix wrong = cc;
+        wrong.values[0] += 1.0;
+        REQUIRE(g::validateFull(ca, cb, wrong).passed == 0);
+        const char* path = "shim_test_matrix.mtx";
+        FILE* f = std::fopen(path, "w");
+        REQUIRE(f != nullptr);
+        std::fprintf(f, "%%%%MatrixMarket matrix coordinate real symmetric\n%% c\n3 3 3\n2 1 1.5D0\n3 3 2\n3 1 -4\n");
+        std::fclose(f);
+        const CsrMatrix m = g::readMatrixMarket<CsrMatrix>(path);
+        REQUIRE(m.rows == 3 && m.rowPtr == (std::vector<int64_t>{0, 2, 3, 5}));
+        REQUIRE(m.columnIndices == (std::vector<int>{1, 2, 0, 2, 0}));
+        REQUIRE(m.values == (std::vector<double>{1.5, -4.0, 1.5, 2.0, -4.0}));
+        const CsrMatrix mt = g::transpose(m);
+        REQUIRE(mt.rowPtr == m.rowPtr && mt.columnIndices == m.columnIndices && mt.values == m.values);
+        f = std::fopen(path, "w");
+        std::fprintf(f, "%%%%MatrixMarket matrix coordinate real general\n2 2 1\n3 1 1\n");
+        std::fclose(f);
+        caught = false;
+        try {
+            g::readMatrixMarket<CsrMatrix>(path);
+        } catch (const std::runtime_error&) {
+            caught = true;
+        }
+        REQUIRE(caught);
+        std::remove(path);
+    }
     std::printf("shim_test: PASS\n");
     return 0;
 }

@@ -19,6 +19,6 @@ def test_cpp_shim(tmp_path):
     subprocess.run(["g++", "-std=c++17", "-O2", f"-I{ROOT / 'include'}", str(ROOT / "tests" / "cpp" / "shim_test.cpp"),
                     f"-L{lib_dir}", "-lspgemm_gb300", "-o", str(exe)], check=True)
     env = dict(os.environ, LD_LIBRARY_PATH=f"{lib_dir}:{os.environ.get('LD_LIBRARY_PATH', '')}")
-    r = subprocess.run([str(exe)], capture_output=True, text=True, env=env, timeout=300)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, env=env, timeout=300, cwd=str(tmp_path))
     assert r.returncode == 0, r.stdout + r.stderr
     assert "PASS" in r.stdout
