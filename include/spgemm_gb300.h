@@ -89,7 +89,9 @@ typedef struct {
     int64_t bin_rows[20];        /* rows per product-count bin: empty, <=32, 64, 96, 128, 192, 256, 384, 512,
                                     768, 1024, 1536, 2048, 3072, 4096, 6144, 8192, 12288, 16384, heavier */
     int64_t launches;            /* kernels this library launched for the call */
-    float ms_numeric_bin[20];    /* numeric-phase time of each bin (same order as bin_rows) */
+    float ms_numeric_bin[20];    /* per bin (same order as bin_rows): time from the start of the numeric
+                                    phase to the end of the bin's launch (bins run on three streams at
+                                    once); spg_tune runs them one after the other and times each */
 } spg_timings;
 
 typedef struct spg_handle spg_handle;

@@ -33,6 +33,12 @@ struct spg_handle {
     std::string err;
     cudaEvent_t ev[6] = {};
     cudaEvent_t bin_ev[kNumBins] = {};  // end of each bin's numeric launch
+    // numeric bins run on three streams (warp bins on `stream`; shared-memory
+    // CTA bins; slab and heavy bins, which share the scratch), so that one
+    // launch's tail overlaps the others; fork/join events
+    cudaStream_t aux[2] = {};
+    cudaEvent_t fork = nullptr, join[2] = {};
+    bool serial_bins = false;  // spg_tune times bins one after the other
     spg_timings last{};
     // accumulate mode: the running sum S (device result) and its shape
     bool acc_active = false;
@@ -367,11 +373,27 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
         jobs[j].holes = exact ? 0 : 1;
     }
     check_cuda(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(Job) * njobs, cudaMemcpyHostToDevice, st), "H2D jobs");
-    for (int b = 1; b < kNumBins; ++b) {
+    // bins from the largest rows down on each stream, so that long launches start first
+    auto stream_of = [&](int b) {
+        if (h->serial_bins) return st;
+        return b <= kLastWarpBin ? st : (b <= kLastSmemBin ? h->aux[0] : h->aux[1]);
+    };
+    if (!h->serial_bins) {
+        cudaEventRecord(h->fork, st);
+        for (cudaStream_t a : h->aux) cudaStreamWaitEvent(a, h->fork, 0);
+    }
+    for (int b = kNumBins - 1; b >= 1; --b) {
         if (!bin_count[b]) continue;
+        cudaStream_t bs = stream_of(b);
         launch_numeric(b, d_jobs, items + bin_off[b], bin_count[b], max_ub, scratch, scratch_bytes, &d_ctrl->stats,
-                       &d_ctrl->err, st, h->num_sms, !exact, h->bin_variant[b]);
-        cudaEventRecord(h->bin_ev[b], st);
+                       &d_ctrl->err, bs, h->num_sms, !exact, h->bin_variant[b]);
+        cudaEventRecord(h->bin_ev[b], bs);
+    }
+    if (!h->serial_bins) {
+        for (int i = 0; i < 2; ++i) {
+            cudaEventRecord(h->join[i], h->aux[i]);
+            cudaStreamWaitEvent(st, h->join[i], 0);
+        }
     }
     check_cuda(cudaGetLastError(), "K4 launch");
     cudaEventRecord(h->ev[4], st);
@@ -471,12 +493,14 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
     h->last.ms_numeric = elapsed(h->ev[3], h->ev[4]);
     h->last.ms_compact = elapsed(h->ev[4], h->ev[5]);
     h->last.ms_total = elapsed(h->ev[0], h->ev[5]);
+    // per-bin times: launch to launch when the bins ran in sequence (spg_tune),
+    // else the time from the fork to the end of each bin
     cudaEvent_t prev = h->ev[3];
-    for (int b = 0; b < kNumBins; ++b) {
+    for (int b = kNumBins - 1; b >= 0; --b) {
         h->last.ms_numeric_bin[b] = 0.0f;
         if (b == kBinEmpty || !bin_count[b]) continue;
         h->last.ms_numeric_bin[b] = elapsed(prev, h->bin_ev[b]);
-        prev = h->bin_ev[b];
+        if (h->serial_bins) prev = h->bin_ev[b];
     }
     h->last.products = products;
     h->last.nnz = nz_total;
@@ -591,6 +615,9 @@ spg_status spg_create(const spg_config* config, spg_handle** out) {
     cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
     for (auto& e : h->ev) cudaEventCreate(&e);
     for (auto& e : h->bin_ev) cudaEventCreate(&e);
+    for (auto& a : h->aux) cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking);
+    cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming);
+    for (auto& e : h->join) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
     cudaMemPool_t pool;
     if (cudaDeviceGetDefaultMemPool(&pool, h->device) == cudaSuccess) {
         uint64_t threshold = UINT64_MAX;
@@ -612,6 +639,12 @@ void spg_destroy(spg_handle* h) {
     if (h->host_scratch) cudaFreeHost(h->host_scratch);
     for (auto& e : h->ev) cudaEventDestroy(e);
     for (auto& e : h->bin_ev) cudaEventDestroy(e);
+    for (auto a : h->aux) {
+        cudaStreamSynchronize(a);
+        cudaStreamDestroy(a);
+    }
+    cudaEventDestroy(h->fork);
+    for (auto e : h->join) cudaEventDestroy(e);
     cudaStreamDestroy(h->stream);
     cudaFreeHost(h->ctrl);
     delete h;
@@ -819,6 +852,11 @@ spg_status spg_tune(spg_handle* h, const spg_csr_view* A, const spg_csr_view* B,
         uint8_t saved[kNumBins];
         std::memcpy(saved, h->bin_variant, sizeof saved);
         spg_tune_report rep{};
+        struct SerialBins {  // per-bin times need the bins one after the other
+            spg_handle* h;
+            explicit SerialBins(spg_handle* x) : h(x) { h->serial_bins = true; }
+            ~SerialBins() { h->serial_bins = false; }
+        } serial(h);
         try {
             std::vector<JobIn> in{{A, B, CsrView{}}};
             for (int v = 0; v < kNumVariants; ++v) {
@@ -1239,10 +1277,19 @@ void plan_build(spg_plan* p, int32_t n, const spg_csr_view* A, const spg_csr_vie
     check_cuda(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed), "begin capture");
     cudaMemsetAsync(nz, 0, slots * sizeof(int64_t), st);
     cudaMemsetAsync(d_ctrl, 0, sizeof(Ctrl), st);
-    for (int b = 1; b < kNumBins; ++b)
+    // the bins on three streams, as in run_products (the fork/join is part of the graph)
+    cudaEventRecord(h->fork, st);
+    for (cudaStream_t a : h->aux) cudaStreamWaitEvent(a, h->fork, 0);
+    for (int b = kNumBins - 1; b >= 1; --b)
         if (bin_count[b])
             launch_numeric(b, d_jobs, items + bin_off[b], bin_count[b], max_ub, scratch, scratch_bytes,
-                           &d_ctrl->stats, &d_ctrl->err, st, h->num_sms, true, h->bin_variant[b]);
+                           &d_ctrl->stats, &d_ctrl->err,
+                           b <= kLastWarpBin ? st : (b <= kLastSmemBin ? h->aux[0] : h->aux[1]), h->num_sms, true,
+                           h->bin_variant[b]);
+    for (int i = 0; i < 2; ++i) {
+        cudaEventRecord(h->join[i], h->aux[i]);
+        cudaStreamWaitEvent(st, h->join[i], 0);
+    }
     launch_scan(nz, static_cast<int64_t>(slots) - 1, partials, st);
     launch_compact_holes(d_jobs, n, d_row_base, total_rows, p->col, p->val, st);
     launch_gather(nz, d_idx, d_starts, n, st);
