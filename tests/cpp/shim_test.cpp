@@ -99,8 +99,11 @@ int main() {
         REQUIRE(m.rows == 3 && m.rowPtr == (std::vector<int64_t>{0, 2, 3, 5}));
         REQUIRE(m.columnIndices == (std::vector<int>{1, 2, 0, 2, 0}));
         REQUIRE(m.values == (std::vector<double>{1.5, -4.0, 1.5, 2.0, -4.0}));
+        // A^T lists each column of A by increasing row: row 2 becomes (0, 2), not the file order (2, 0)
         const CsrMatrix mt = g::transpose(m);
-        REQUIRE(mt.rowPtr == m.rowPtr && mt.columnIndices == m.columnIndices && mt.values == m.values);
+        REQUIRE(mt.rowPtr == (std::vector<int64_t>{0, 2, 3, 5}));
+        REQUIRE(mt.columnIndices == (std::vector<int>{1, 2, 0, 0, 2}));
+        REQUIRE(mt.values == (std::vector<double>{1.5, -4.0, 1.5, -4.0, 2.0}));
         f = std::fopen(path, "w");
         std::fprintf(f, "%%%%MatrixMarket matrix coordinate real general\n2 2 1\n3 1 1\n");
         std::fclose(f);
