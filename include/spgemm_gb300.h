@@ -80,6 +80,8 @@ typedef struct {
     int32_t device;             /* CUDA device ordinal */
     int32_t mode;               /* spg_mode */
     uint64_t hbm_budget_bytes;  /* largest device footprint a request may reserve; 0 = no limit */
+    int32_t bin_streams;        /* streams the numeric bins of one call spread over: 1, or 3 (0 = 3) */
+    int32_t reserved;
 } spg_config;
 
 /* Per-phase device times of the last multiply on a handle (CUDA events). */

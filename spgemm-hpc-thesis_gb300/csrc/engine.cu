@@ -39,6 +39,7 @@ struct spg_handle {
     cudaStream_t aux[2] = {};
     cudaEvent_t fork = nullptr, join[2] = {};
     bool serial_bins = false;  // spg_tune times bins one after the other
+    bool one_bin_stream = false;  // spg_config.bin_streams == 1
     spg_timings last{};
     // accumulate mode: the running sum S (device result) and its shape
     bool acc_active = false;
@@ -374,11 +375,12 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
     }
     check_cuda(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(Job) * njobs, cudaMemcpyHostToDevice, st), "H2D jobs");
     // bins from the largest rows down on each stream, so that long launches start first
+    const bool one_stream = h->serial_bins || h->one_bin_stream;
     auto stream_of = [&](int b) {
-        if (h->serial_bins) return st;
+        if (one_stream) return st;
         return b <= kLastWarpBin ? st : (b <= kLastSmemBin ? h->aux[0] : h->aux[1]);
     };
-    if (!h->serial_bins) {
+    if (!one_stream) {
         cudaEventRecord(h->fork, st);
         for (cudaStream_t a : h->aux) cudaStreamWaitEvent(a, h->fork, 0);
     }
@@ -389,7 +391,7 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
                        &d_ctrl->err, bs, h->num_sms, !exact, h->bin_variant[b]);
         cudaEventRecord(h->bin_ev[b], bs);
     }
-    if (!h->serial_bins) {
+    if (!one_stream) {
         for (int i = 0; i < 2; ++i) {
             cudaEventRecord(h->join[i], h->aux[i]);
             cudaStreamWaitEvent(st, h->join[i], 0);
@@ -500,7 +502,7 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
         h->last.ms_numeric_bin[b] = 0.0f;
         if (b == kBinEmpty || !bin_count[b]) continue;
         h->last.ms_numeric_bin[b] = elapsed(prev, h->bin_ev[b]);
-        if (h->serial_bins) prev = h->bin_ev[b];
+        if (one_stream) prev = h->bin_ev[b];
     }
     h->last.products = products;
     h->last.nnz = nz_total;
@@ -603,9 +605,11 @@ spg_status spg_create(const spg_config* config, spg_handle** out) {
         return SPG_CUDA_ERROR;
     }
     if (cfg.device < 0 || cfg.device >= ndev) return SPG_INVALID_ARGUMENT;
+    if (cfg.bin_streams != 0 && cfg.bin_streams != 1 && cfg.bin_streams != 3) return SPG_INVALID_ARGUMENT;
     auto* h = new spg_handle;
     h->cfg = cfg;
     h->device = cfg.device;
+    h->one_bin_stream = cfg.bin_streams == 1;
     if (cudaSetDevice(h->device) != cudaSuccess || cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMallocHost(&h->ctrl, kCtrlBytes) != cudaSuccess) {
         cudaGetLastError();

@@ -307,6 +307,7 @@ spg_status spg_server_create(const spg_server_config* config, spg_server** out) 
         spg_config_default(&hc);
         hc.device = cfg.device;
         hc.mode = cfg.mode;
+        hc.bin_streams = cfg.lanes > 1 ? 1 : 0;  // the lanes already overlap batches on the device
         spg_handle* h = nullptr;
         const spg_status st = spg_create(&hc, &h);
         if (st != SPG_OK) {

@@ -91,7 +91,8 @@ class _Result(C.Structure):
 
 
 class _Config(C.Structure):
-    _fields_ = [("device", C.c_int32), ("mode", C.c_int32), ("hbm_budget_bytes", C.c_uint64)]
+    _fields_ = [("device", C.c_int32), ("mode", C.c_int32), ("hbm_budget_bytes", C.c_uint64),
+                ("bin_streams", C.c_int32), ("reserved", C.c_int32)]
 
 
 MODES = {"auto": 0, "exact": 1, "upper_bound": 2}
@@ -247,9 +248,9 @@ def _take_host(res: _Result, engine: "Engine") -> Csr:
 class Engine:
     """One engine handle (one CUDA stream and its workspace) on one device."""
 
-    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0, mode: str = "auto"):
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0, mode: str = "auto", bin_streams: int = 0):
         lib = library()
-        cfg = _Config(device, MODES[mode], hbm_budget_bytes)
+        cfg = _Config(device, MODES[mode], hbm_budget_bytes, bin_streams, 0)
         h = C.c_void_p()
         st = lib.spg_create(C.byref(cfg), C.byref(h))
         if st != 0:
