@@ -384,7 +384,10 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
         cudaEventRecord(h->fork, st);
         for (cudaStream_t a : h->aux) cudaStreamWaitEvent(a, h->fork, 0);
     }
-    for (int b = kNumBins - 1; b >= 1; --b) {
+    // on three streams each stream starts with its largest rows; on one stream the
+    // bins go from the smallest rows up (measured faster for overlapping server lanes)
+    for (int i = 1; i < kNumBins; ++i) {
+        const int b = one_stream ? i : kNumBins - i;
         if (!bin_count[b]) continue;
         cudaStream_t bs = stream_of(b);
         launch_numeric(b, d_jobs, items + bin_off[b], bin_count[b], max_ub, scratch, scratch_bytes, &d_ctrl->stats,
@@ -498,12 +501,14 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
     // per-bin times: launch to launch when the bins ran in sequence (spg_tune),
     // else the time from the fork to the end of each bin
     cudaEvent_t prev = h->ev[3];
-    for (int b = kNumBins - 1; b >= 0; --b) {
+    for (int i = 1; i < kNumBins; ++i) {
+        const int b = one_stream ? i : kNumBins - i;
         h->last.ms_numeric_bin[b] = 0.0f;
-        if (b == kBinEmpty || !bin_count[b]) continue;
+        if (!bin_count[b]) continue;
         h->last.ms_numeric_bin[b] = elapsed(prev, h->bin_ev[b]);
         if (one_stream) prev = h->bin_ev[b];
     }
+    h->last.ms_numeric_bin[kBinEmpty] = 0.0f;
     h->last.products = products;
     h->last.nnz = nz_total;
     h->last.rows = total_rows;
