@@ -110,7 +110,6 @@ struct spg_server {
     uint64_t next_batch = 1;
     int64_t in_use = 0;
     bool stop = false;
-    std::string err;
 
     void lane_main(int lane);
     void run_batch(int lane, std::vector<Request*>& batch);
@@ -229,13 +228,9 @@ void spg_server::lane_main(int lane) {
         // 2. admission: the longest FIFO prefix that fits the free budget
         std::vector<Request*> batch;
         int64_t fp = 0, batch_products = 0;
-        bool blocked = false;
         for (auto it = pending.begin(); it != pending.end();) {
             Request* r = *it;
-            if (r->products < 0) {  // still being counted by another lane: keep the order
-                blocked = true;
-                break;
-            }
+            if (r->products < 0) break;  // still being counted by another lane: keep the order
             if (r->footprint > budget) {  // can never fit
                 it = pending.erase(it);
                 finish_request(r, SPG_BUDGET_EXCEEDED,
@@ -243,10 +238,7 @@ void spg_server::lane_main(int lane) {
                 cv.notify_all();
                 continue;
             }
-            if (in_use + fp + r->footprint > budget) {
-                blocked = true;
-                break;
-            }
+            if (in_use + fp + r->footprint > budget) break;  // wait for memory: FIFO order
             if (!batch.empty() && batch_products + r->products > cfg.max_batch_products) break;
             batch.push_back(r);
             fp += r->footprint;
@@ -255,7 +247,6 @@ void spg_server::lane_main(int lane) {
             if (static_cast<int>(batch.size()) >= cfg.max_batch) break;
         }
         if (batch.empty()) {
-            (void)blocked;
             cv.wait(lk);  // new arrivals, a finished batch, a finished count or shutdown
             continue;
         }
