@@ -124,10 +124,10 @@ spg_status spg_multiply(spg_handle* handle, const spg_csr_view* A, const spg_csr
 
 /* C = A * B written into caller host arrays: row_ptr of A.rows+1 entries,
  * col/val of c_capacity entries (nnz(C) <= the scalar-product count, so that
- * count is always enough).  The product runs in row blocks of about 2^27
- * scalar products; the device->host copy of each finished block runs on a
- * second stream while later blocks compute, so the transfer of C overlaps the
- * computation.  Page-locked buffers (spg_host_alloc) are needed for the
+ * count is always enough).  When A has 2^22 entries or more the product runs
+ * in row blocks holding 1/32, 1/32, 1/16, then 1/8 of A's entries each; the
+ * device->host copy of each finished block runs on a second stream while the
+ * later blocks compute, so the transfer of C overlaps the computation.  Page-locked buffers (spg_host_alloc) are needed for the
  * overlap; pageable ones work but copy synchronously.  *c_nnz receives nnz(C);
  * if it exceeds c_capacity the call fails with SPG_BUDGET_EXCEEDED and *c_nnz
  * holds a lower bound of the entries needed.  Results are those of

@@ -692,9 +692,8 @@ spg_status spg_multiply(spg_handle* h, const spg_csr_view* A, const spg_csr_view
     });
 }
 
-// Row blocks of about kChunkProducts scalar products each (at most kMaxChunks).
-constexpr int64_t kChunkProducts = int64_t{1} << 27;
-constexpr int kMaxChunks = 16;
+// Operands with at least this many entries in A are multiplied in row blocks.
+constexpr int64_t kBlockedEntries = int64_t{1} << 22;
 
 spg_status spg_multiply_to_host(spg_handle* h, const spg_csr_view* A, const spg_csr_view* B, int64_t* c_row_ptr,
                                 int32_t* c_col, double* c_val, int64_t c_capacity, int64_t* c_nnz) {
@@ -727,17 +726,35 @@ spg_status spg_multiply_to_host(spg_handle* h, const spg_csr_view* A, const spg_
                 }
             }
         }
-        // row blocks: equal numbers of rows, about kChunkProducts products each
-        int64_t products = 0;
-        {
-            std::vector<JobIn> in{{&dv[0], &dv[1], CsrView{}}};
-            std::vector<DevResult> none;
-            run_products(h, in, none, true, &products);
-        }
+        // Row blocks by A's entries: 1/32, 1/32, 1/16, then 1/8 each, so that the first
+        // copy starts after a small block and the later blocks keep the copy engine
+        // busy while the next one computes.  Small operands run as one block.  The
+        // cuts come from A's row offsets on the host, or from equal row counts
+        // when A lives on the device.
         const int32_t m = A->rows;
-        const int nchunks = static_cast<int>(
-            std::max<int64_t>(1, std::min<int64_t>({kMaxChunks, (products + kChunkProducts - 1) / kChunkProducts,
-                                                    static_cast<int64_t>(m)})));
+        std::vector<int32_t> cut{0};
+        if (A->nnz >= kBlockedEntries && m > 1) {
+            const double fr[] = {1.0 / 32, 1.0 / 32, 1.0 / 16, 1.0 / 8, 1.0 / 8, 1.0 / 8, 1.0 / 8,
+                                 1.0 / 8, 1.0 / 8, 1.0 / 8};
+            double acc = 0.0;
+            for (double f : fr) {
+                acc += f;
+                int32_t r;
+                if (acc >= 1.0 - 1e-12) {
+                    r = m;
+                } else if (A->location == SPG_HOST) {
+                    const int64_t target = static_cast<int64_t>(acc * static_cast<double>(A->nnz));
+                    r = static_cast<int32_t>(std::lower_bound(A->row_ptr, A->row_ptr + m + 1, target) - A->row_ptr);
+                } else {
+                    r = static_cast<int32_t>(acc * m);
+                }
+                r = std::min(std::max(r, cut.back()), m);
+                if (r > cut.back()) cut.push_back(r);
+            }
+        }
+        if (cut.back() != m) cut.push_back(m);
+        const int nchunks = static_cast<int>(cut.size()) - 1;
+        int64_t products = 0;
         spg_timings sum{};
         int64_t off = 0;
         std::vector<cudaEvent_t> done;
@@ -755,8 +772,7 @@ spg_status spg_multiply_to_host(spg_handle* h, const spg_csr_view* A, const spg_
         };
         c_row_ptr[0] = 0;
         for (int k = 0; k < nchunks; ++k) {
-            const int32_t r0 = static_cast<int32_t>(static_cast<int64_t>(m) * k / nchunks);
-            const int32_t r1 = static_cast<int32_t>(static_cast<int64_t>(m) * (k + 1) / nchunks);
+            const int32_t r0 = cut[k], r1 = cut[k + 1];
             spg_csr_view blk = dv[0];
             blk.rows = r1 - r0;
             blk.row_ptr = dv[0].row_ptr + r0;  // absolute offsets into A's column/value arrays
@@ -796,6 +812,7 @@ spg_status spg_multiply_to_host(spg_handle* h, const spg_csr_view* A, const spg_
             sum.ms_compact += h->last.ms_compact;
             sum.ms_total += h->last.ms_total;
             sum.launches += h->last.launches + 1;
+            products += r.products;
             for (int b = 0; b < kNumBins; ++b) {
                 sum.bin_rows[b] += h->last.bin_rows[b];
                 sum.ms_numeric_bin[b] += h->last.ms_numeric_bin[b];

@@ -36,7 +36,7 @@ def test_small_product_matches_reference(engine, port):
 
 @pytest.mark.parametrize("pinned", [False, True])
 def test_row_blocks_match_single_call(engine, pinned):
-    # 152 M scalar products: three row blocks of about 2^26
+    # 6.3 M entries in A: ten row blocks
     a = synth_powerlaw(262144, 24.0, 1.2, 20000, 2048, 0.7, seed=3)
     got = to_host(engine, a, a, pinned=pinned)
     assert engine.last_timings()["products"] == engine.scalar_multiplication_count(a, a)

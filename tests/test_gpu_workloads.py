@@ -151,7 +151,7 @@ def test_powerlaw_exact_mode_full_validation(port, powerlaw):
 
 
 def test_powerlaw_to_host_full_validation(engine, powerlaw):
-    # the overlapped row-block path at full size (5 row blocks), checked on the GPU
+    # the overlapped row-block path at full size (10 row blocks), checked on the GPU
     import torch
     p = engine.scalar_multiplication_count(powerlaw, powerlaw)
     rp = torch.empty(powerlaw.rows + 1, dtype=torch.int64, pin_memory=True)
