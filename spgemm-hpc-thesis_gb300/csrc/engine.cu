@@ -342,10 +342,35 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
     for (int b = 1; b < kNumBins; ++b) launches += bin_count[b] > 0 ? (exact ? 2 : 1) : 0;
     launches += 3;  // scan
     int64_t tmp_total = products;
+    // The bins of K2 and K4 run on three streams (warp bins; shared-memory CTA
+    // bins; slab and heavy bins, which share the scratch), forked from and
+    // joined back into the main stream, so that the tail of one launch overlaps
+    // the others.  On one stream (server lanes, the tuner) they run in order.
+    const bool one_stream = h->serial_bins || h->one_bin_stream;
+    auto stream_of = [&](int b) {
+        if (one_stream) return st;
+        return b <= kLastWarpBin ? st : (b <= kLastSmemBin ? h->aux[0] : h->aux[1]);
+    };
+    auto fork = [&] {
+        if (one_stream) return;
+        cudaEventRecord(h->fork, st);
+        for (cudaStream_t a : h->aux) cudaStreamWaitEvent(a, h->fork, 0);
+    };
+    auto join = [&] {
+        if (one_stream) return;
+        for (int i = 0; i < 2; ++i) {
+            cudaEventRecord(h->join[i], h->aux[i]);
+            cudaStreamWaitEvent(st, h->join[i], 0);
+        }
+    };
     if (exact) {
-        for (int b = 1; b < kNumBins; ++b)
+        fork();
+        for (int i = 1; i < kNumBins; ++i) {
+            const int b = one_stream ? i : kNumBins - i;
             launch_symbolic(b, d_jobs, items + bin_off[b], bin_count[b], max_ub, scratch, scratch_bytes,
-                            &d_ctrl->stats, &d_ctrl->err, st, h->num_sms);
+                            &d_ctrl->stats, &d_ctrl->err, stream_of(b), h->num_sms);
+        }
+        join();
         check_cuda(cudaGetLastError(), "K2 launch");
     }
     cudaEventRecord(h->ev[2], st);
@@ -374,16 +399,7 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
         jobs[j].holes = exact ? 0 : 1;
     }
     check_cuda(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(Job) * njobs, cudaMemcpyHostToDevice, st), "H2D jobs");
-    // bins from the largest rows down on each stream, so that long launches start first
-    const bool one_stream = h->serial_bins || h->one_bin_stream;
-    auto stream_of = [&](int b) {
-        if (one_stream) return st;
-        return b <= kLastWarpBin ? st : (b <= kLastSmemBin ? h->aux[0] : h->aux[1]);
-    };
-    if (!one_stream) {
-        cudaEventRecord(h->fork, st);
-        for (cudaStream_t a : h->aux) cudaStreamWaitEvent(a, h->fork, 0);
-    }
+    fork();
     // on three streams each stream starts with its largest rows; on one stream the
     // bins go from the smallest rows up (measured faster for overlapping server lanes)
     for (int i = 1; i < kNumBins; ++i) {
@@ -394,12 +410,7 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
                        &d_ctrl->err, bs, h->num_sms, !exact, h->bin_variant[b]);
         cudaEventRecord(h->bin_ev[b], bs);
     }
-    if (!one_stream) {
-        for (int i = 0; i < 2; ++i) {
-            cudaEventRecord(h->join[i], h->aux[i]);
-            cudaStreamWaitEvent(st, h->join[i], 0);
-        }
-    }
+    join();
     check_cuda(cudaGetLastError(), "K4 launch");
     cudaEventRecord(h->ev[4], st);
     launch_readback(d_ctrl, hc, sizeof(Ctrl), st);

@@ -7,9 +7,11 @@
 //   * rows of <= 32 products: one warp, one product per lane, distinct columns
 //     found with __match_any_sync (no table);
 //   * rows of <= 512 products: one warp per row, table in shared memory;
-//   * rows of <= 8192 products: one CTA per row, table in shared memory;
+//   * rows of <= 16384 products: one CTA per row, table in shared memory;
 //   * heavier rows: one CTA per row, table in a global-memory slab per CTA.
-// It also rejects B columns outside [0, B.cols).
+// Every launch reserves the tables of its bin's largest row only (a power of
+// two >= twice the bin capacity), so that the bins of short rows keep many
+// CTAs per SM.  It also rejects B columns outside [0, B.cols).
 #include <algorithm>
 
 #include "spg_enum.cuh"
@@ -18,10 +20,22 @@ namespace spg {
 namespace {
 
 constexpr int kSymWarpThreads = 256;
-constexpr int kSymWarpTable = 1024;   // slots per warp (rows of <= 512 products)
-constexpr int kSymBlockThreads = 256;
-constexpr int kSymBlockTable = 16384; // slots per CTA (rows of <= 8192 products)
 constexpr int kSymHeavyThreads = 512;
+constexpr int kLastSymSmemBin = 18;  // rows of <= 16384 products: shared-memory tables
+#ifndef SPG_SYM_B64
+#define SPG_SYM_B64 10
+#endif
+#ifndef SPG_SYM_B128
+#define SPG_SYM_B128 12
+#endif
+
+// Table slots reserved per row (warp bins) or per CTA (CTA bins) for bin b:
+// the power of two >= twice its capacity, at least 64.
+int sym_table_slots(int b) {
+    int64_t t = 64;
+    while (t < 2 * bin_capacity(b)) t *= 2;
+    return static_cast<int>(t);
+}
 
 __device__ inline bool col_ok(int32_t c, int32_t cols, ErrWord* err) {
     if (c < 0 || c >= cols) {
@@ -44,8 +58,8 @@ __device__ inline int hash_insert(int32_t* tab, uint32_t mask, int log2t, int32_
 
 __global__ void __launch_bounds__(kSymWarpThreads)
 sym_warp_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items, int64_t count, int tiny,
-                ErrWord* __restrict__ err) {
-    __shared__ int32_t s_tab[kSymWarpThreads / 32][kSymWarpTable];
+                int wtab, ErrWord* __restrict__ err) {
+    extern __shared__ int32_t s_dyn[];  // kSymWarpThreads / 32 tables of wtab slots
     __shared__ SegTab<32, int32_t> s_seg[kSymWarpThreads / 32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t warps = static_cast<int64_t>(gridDim.x) * (kSymWarpThreads / 32);
@@ -57,7 +71,7 @@ sym_warp_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items,
         int found = 0;
         if (tiny) {
             // <= 32 products: product t goes to lane t; count the first lane of each column group.
-            int32_t* stage = s_tab[w];
+            int32_t* stage = s_dyn + w * wtab;
             team_products<32, false, int32_t>(J, row, s_seg[w], nullptr, lane, [&](int32_t seq, int32_t c, double, double) {
                 stage[seq] = c;
             });
@@ -72,7 +86,7 @@ sym_warp_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items,
         } else {
             const int log2t = max(6, ceil_log2(2 * ub));
             const uint32_t tsize = 1u << log2t, mask = tsize - 1;
-            int32_t* tab = s_tab[w];
+            int32_t* tab = s_dyn + w * wtab;
             for (uint32_t s = lane; s < tsize; s += 32) tab[s] = -1;
             __syncwarp();
             int mine = 0;
@@ -86,12 +100,13 @@ sym_warp_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items,
     }
 }
 
-__global__ void __launch_bounds__(kSymBlockThreads)
+template <int NT>
+__global__ void __launch_bounds__(NT)
 sym_block_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items, int64_t count,
                  ErrWord* __restrict__ err) {
-    extern __shared__ int32_t s_tab[];  // kSymBlockTable slots
-    __shared__ SegTab<kSymBlockThreads, int32_t> s_seg;
-    __shared__ int64_t s_warp[kSymBlockThreads / 32 + 1];
+    extern __shared__ int32_t s_tab[];  // the bin's table slots
+    __shared__ SegTab<NT, int32_t> s_seg;
+    __shared__ int64_t s_warp[NT / 32 + 1];
     __shared__ int s_found;
     for (int64_t i = blockIdx.x; i < count; i += gridDim.x) {
         const int64_t it = items[i];
@@ -99,11 +114,11 @@ sym_block_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items
         const int row = item_row(it);
         const int log2t = max(6, ceil_log2(2 * J.ub[row]));
         const uint32_t tsize = 1u << log2t, mask = tsize - 1;
-        for (uint32_t s = threadIdx.x; s < tsize; s += kSymBlockThreads) s_tab[s] = -1;
+        for (uint32_t s = threadIdx.x; s < tsize; s += NT) s_tab[s] = -1;
         if (threadIdx.x == 0) s_found = 0;
         __syncthreads();
         int mine = 0;
-        team_products<kSymBlockThreads, false, int32_t>(J, row, s_seg, s_warp, threadIdx.x,
+        team_products<NT, false, int32_t>(J, row, s_seg, s_warp, threadIdx.x,
                                                         [&](int32_t, int32_t c, double, double) {
             if (col_ok(c, J.B.cols, err)) mine += hash_insert(s_tab, mask, log2t, c);
         });
@@ -154,8 +169,7 @@ int heavy_ctas(int64_t count, int num_sms) { return static_cast<int>(count < num
 }  // namespace
 
 size_t symbolic_scratch_bytes(const int64_t* bin_count, int64_t max_ub, int num_sms) {
-    int64_t count = 0;  // the global-hash bins run one after the other
-    for (int b = kLastSmemBin + 1; b < kNumBins; ++b) count = std::max(count, bin_count[b]);
+    const int64_t count = bin_count[kBinHeavy];  // the only bin with global-memory tables
     if (count == 0) return 0;
     return static_cast<size_t>(heavy_ctas(count, num_sms)) * (size_t{1} << ceil_log2(2 * max_ub)) * sizeof(int32_t);
 }
@@ -164,13 +178,22 @@ void launch_symbolic(int bin, const Job* d_jobs, const int64_t* d_items, int64_t
                      void* d_scratch, size_t, Stats*, ErrWord* d_err, cudaStream_t stream, int num_sms) {
     if (count <= 0) return;
     if (bin <= kLastWarpBin) {
+        const int wtab = sym_table_slots(bin);
+        const int smem = (kSymWarpThreads / 32) * wtab * static_cast<int>(sizeof(int32_t));
+        cudaFuncSetAttribute(sym_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         const int grid = capped_grid(count, kSymWarpThreads / 32, num_sms * 32);
-        sym_warp_kernel<<<grid, kSymWarpThreads, 0, stream>>>(d_jobs, d_items, count, bin == 1, d_err);
-    } else if (bin <= kLastSmemBin) {
-        const int smem = kSymBlockTable * sizeof(int32_t);
-        cudaFuncSetAttribute(sym_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        const int grid = capped_grid(count, 1, num_sms * 8);
-        sym_block_kernel<<<grid, kSymBlockThreads, smem, stream>>>(d_jobs, d_items, count, d_err);
+        sym_warp_kernel<<<grid, kSymWarpThreads, smem, stream>>>(d_jobs, d_items, count, bin == 1, wtab, d_err);
+    } else if (bin <= kLastSymSmemBin) {
+        const int smem = sym_table_slots(bin) * static_cast<int>(sizeof(int32_t));
+        auto run = [&](auto kernel, int nt) {
+            cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            kernel<<<capped_grid(count, 1, num_sms * (2048 / nt)), nt, smem, stream>>>(d_jobs, d_items, count, d_err);
+        };
+        // CTA size by row size: 6-12 products per thread on the bins below 4096 products
+        if (bin <= SPG_SYM_B64) run(sym_block_kernel<64>, 64);
+        else if (bin <= SPG_SYM_B128) run(sym_block_kernel<128>, 128);
+        else if (bin <= kLastSmemBin) run(sym_block_kernel<256>, 256);
+        else run(sym_block_kernel<512>, 512);
     } else {
         const int grid = heavy_ctas(count, num_sms);
         const int64_t slots = int64_t{1} << ceil_log2(2 * max_ub);
