@@ -411,7 +411,7 @@ void launch_numeric(int bin, const Job* d_jobs, const int64_t* d_items, int64_t 
         case 9: run_block<3, 8, 8>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;     // <= 768
         case 10: run_block<2, 16, 8>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;   // <= 1024
         case 11: run_block<6, 8, 4>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;    // <= 1536
-        case 12: run_block<8, 8, 3>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;    // <= 2048
+        case 12: run_block<8, 8, 4>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;    // <= 2048
         case 13: run_block<12, 8, 2>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;   // <= 3072
         case 14: run_block<8, 16, 2>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;   // <= 4096
         case 15: run_block<16, 12, 1>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;  // <= 6144

@@ -437,8 +437,14 @@ __device__ void numeric_row(const Job& J, int row, RowSmem<W, ITEMS, SV>& sm, do
 
 constexpr int kWarpKernelThreads = 256;
 
+// Resident CTAs per SM the warp-row kernels are compiled for (caps registers
+// at 80 and 64 per thread).  Measured on power-law rows, one bin at a time:
+// the 12- and 16-item kernels 0.92 / 0.85 -> 0.79 / 0.80 ms against 2 CTAs
+// (128 registers), the 6- and 8-item ones 0.39 -> 0.35 ms against 3.
+constexpr int warp_kernel_min_blocks(int items) { return items >= 12 ? 3 : 4; }
+
 template <int ITEMS>
-__global__ void __launch_bounds__(kWarpKernelThreads)
+__global__ void __launch_bounds__(kWarpKernelThreads, warp_kernel_min_blocks(ITEMS))
 num_warp_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items, int64_t count,
                 Stats* __restrict__ stats, ErrWord* __restrict__ err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];

@@ -10,9 +10,9 @@
 // Segments are processed in batches of one per thread: the batch's segment
 // lengths are scanned and its descriptors staged in shared memory.  The team's
 // threads then stride over the batch's products (neighbouring threads read
-// neighbouring B entries, coalesced), four products per thread at a time: each
-// of the four finds its segment by binary search, then the four column and four
-// value loads are issued together, so a thread keeps eight independent global
+// neighbouring B entries, coalesced), U products per thread at a time (four by
+// default): each finds its segment by binary search, then their column and
+// value loads are issued together, so a thread keeps 2U independent global
 // loads in flight instead of one.
 #pragma once
 
@@ -22,13 +22,22 @@ namespace spg {
 
 // Idx is int32_t for rows of at most 2^31 - 1 products (every shared-memory
 // path), int64_t otherwise.
+__host__ __device__ constexpr int pow2_ceil_c(int x) { return x <= 1 ? 1 : 2 * pow2_ceil_c((x + 1) / 2); }
+
 template <int N, typename Idx = int64_t>
 struct SegTab {
+    static constexpr int kPad = pow2_ceil_c(N) - N;  // entries past N, above every sequence number
     const int32_t* colp[N];
     const double* valp[N];
     double scale[N];
-    Idx incl[N];  // inclusive prefix of segment lengths within the batch
+    Idx incl[N + kPad];  // inclusive prefix of segment lengths within the batch
 };
+
+// Writes the padding entries of a team's segment table (once per enumeration).
+template <int N, typename Idx>
+__device__ inline void pad_segtab(SegTab<N, Idx>& tab, int tid) {
+    if (SegTab<N, Idx>::kPad && tid < SegTab<N, Idx>::kPad) tab.incl[N + tid] = static_cast<Idx>(INT64_MAX >> (64 - 8 * sizeof(Idx)));
+}
 
 // Segment e of a row (e counts the addend first when present).
 template <typename Idx>
@@ -51,17 +60,16 @@ __device__ inline void row_segment(const Job& J, int row, int64_t a0, bool has_s
     }
 }
 
-__host__ __device__ constexpr int pow2_ceil_c(int x) { return x <= 1 ? 1 : 2 * pow2_ceil_c((x + 1) / 2); }
-
 // Smallest j in [0, N) with incl[j] > t (the batch total exceeds t): the
-// number of entries <= t, by binary lifting over the next power of two (the
-// bound test folds away when N is one).
+// number of entries <= t, by binary lifting over the next power of two.  The
+// table's padding entries (pad_segtab) exceed every t, so no step needs a
+// bound test.
 template <int N, typename Idx>
 __device__ inline int seg_search(const Idx* incl, Idx t) {
     int j = 0;
 #pragma unroll
     for (int step = pow2_ceil_c(N) / 2; step >= 1; step >>= 1)
-        if ((N == pow2_ceil_c(N) || j + step - 1 < N) && incl[j + step - 1] <= t) j += step;
+        if (incl[j + step - 1] <= t) j += step;
     return j;
 }
 
@@ -97,12 +105,14 @@ __device__ inline void team_sync() {
 // a*b).  kLoadVal = false skips the value loads (b is then 0).  Idx is the
 // index type of sequence numbers within the row (int32_t when the row has fewer
 // than 2^31 products, which keeps the per-product search in 32-bit integers).
-template <int NT, bool kLoadVal, typename Idx = int64_t, typename F>
+// U products per thread are resolved and loaded together.
+template <int NT, bool kLoadVal, typename Idx = int64_t, int U = 4, typename F>
 __device__ inline void team_products(const Job& J, int row, SegTab<NT, Idx>& tab, int64_t* s_warp, int tid,
                                      F&& f) {
     const bool has_s = J.S.rp != nullptr;
     const int64_t a0 = J.A.rp[row];
     const int64_t nseg = (J.A.rp[row + 1] - a0) + (has_s ? 1 : 0);
+    pad_segtab(tab, tid);
     Idx seq_base = 0;
     for (int64_t e0 = 0; e0 < nseg; e0 += NT) {
         const int64_t e = e0 + tid;
@@ -120,25 +130,25 @@ __device__ inline void team_products(const Job& J, int row, SegTab<NT, Idx>& tab
         tab.incl[tid] = incl;
         team_sync<NT>();
         const Idx total = tab.incl[NT - 1];
-        for (Idx t0 = tid; t0 < total; t0 += 4 * NT) {
-            int j[4];
-            Idx q[4];
+        for (Idx t0 = tid; t0 < total; t0 += U * NT) {
+            int j[U];
+            Idx q[U];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < U; ++u) {
                 const Idx t = t0 + u * NT;
                 j[u] = t < total ? seg_search<NT>(tab.incl, t) : 0;
                 q[u] = t < total ? t - (j[u] ? tab.incl[j[u] - 1] : Idx{0}) : Idx{0};
             }
-            int32_t c[4];
-            double b[4];
+            int32_t c[U];
+            double b[U];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < U; ++u) {
                 const bool ok = t0 + u * NT < total;
                 c[u] = ok ? __ldg(tab.colp[j[u]] + q[u]) : 0;
                 b[u] = (kLoadVal && ok) ? __ldg(tab.valp[j[u]] + q[u]) : 0.0;
             }
 #pragma unroll
-            for (int u = 0; u < 4; ++u)
+            for (int u = 0; u < U; ++u)
                 if (t0 + u * NT < total) f(seq_base + t0 + u * NT, c[u], b[u], tab.scale[j[u]]);
         }
         seq_base += total;
@@ -164,6 +174,7 @@ __device__ inline void team_products_in(const Job& J, int row, SegTab<NT, int32_
     const bool has_s = J.S.rp != nullptr;
     const int64_t a0 = J.A.rp[row];
     const int64_t nseg = (J.A.rp[row + 1] - a0) + (has_s ? 1 : 0);
+    pad_segtab(tab, tid);
     int32_t kept_base = 0;
     for (int64_t e0 = 0; e0 < nseg; e0 += NT) {
         const int64_t e = e0 + tid;
