@@ -492,8 +492,11 @@ inline int capped(int64_t work, int per_block, int cap) {
     return static_cast<int>(g < 1 ? 1 : (g > cap ? cap : g));
 }
 
-// CTAs of a launch whose CTAs each own a global slab: one per SM at most.
-inline int slab_grid(int64_t count, int num_sms) { return static_cast<int>(count < num_sms ? count : num_sms); }
+// CTAs of a launch whose CTAs each own a global slab: minb per SM at most.
+inline int slab_grid(int64_t count, int num_sms, int minb = 1) {
+    const int64_t cap = static_cast<int64_t>(num_sms) * minb;
+    return static_cast<int>(count < cap ? count : cap);
+}
 
 template <int ITEMS>
 void run_warp(const Job* jobs, const int64_t* items, int64_t count, Stats* stats, ErrWord* err, cudaStream_t st,
@@ -509,7 +512,7 @@ void run_block(const Job* jobs, const int64_t* items, int64_t count, Stats* stat
                int num_sms, double* gvals = nullptr) {
     const int smem = static_cast<int>(sizeof(RowSmem<W, ITEMS, SV>));
     cudaFuncSetAttribute(num_block_kernel<W, ITEMS, MINB, SV>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    const int grid = SV ? capped(count, 1, num_sms * 8) : slab_grid(count, num_sms);
+    const int grid = SV ? capped(count, 1, num_sms * 8) : slab_grid(count, num_sms, MINB);
     num_block_kernel<W, ITEMS, MINB, SV><<<grid, W * 32, smem, st>>>(jobs, items, count, stats, err, gvals);
 }
 

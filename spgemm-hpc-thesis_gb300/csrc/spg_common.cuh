@@ -203,7 +203,8 @@ void launch_numeric_warp(int bin, const Job* d_jobs, const int64_t* d_items, int
                          ErrWord* d_err, cudaStream_t stream, int num_sms);
 // Global scratch of the numeric phase (value slabs of the 16K bin, sort slabs
 // of heavy rows; the two launches run one after the other and share it).
-size_t numeric_scratch_bytes(const int64_t* bin_count, int64_t max_ub, int num_sms, bool holes);
+size_t numeric_scratch_bytes(const int64_t* bin_count, int64_t max_ub, int num_sms, bool holes,
+                             bool concurrent = true);
 // K5: move rows from C_tmp (offsets job.cnt) to C (offsets job.nz, scanned).
 void launch_compact(const Job* d_job, int rows, int32_t* out_col, double* out_val, cudaStream_t stream);
 // K5 for rows written with holes: keeps the slots whose column is >= 0.
