@@ -377,18 +377,25 @@ int heavy_grid(int64_t count, int num_sms) { return static_cast<int>(count < num
 // Product-value slab of one CTA of the two global-slab bins.
 constexpr int64_t slab_cap(int bin) { return bin == 17 ? 16 * 32 * 24 : 16 * 32 * 32; }
 
-// Team shapes of the bins of <= 6144 and <= 8192 products: warps, products per
-// thread, CTAs per SM, product values in shared memory (else in a per-CTA
-// global slab at the end of the scratch).  With its values in a slab the 6144
-// bin fits two CTAs per SM (87 KB of shared memory each), so one CTA's barrier
-// no longer idles the SM: 1.55 -> 1.34 ms on the power-law workload.  The 8192
-// bin measured the same either way and keeps its values in shared memory.
+// Team shapes of the bins of 2049-8192 products: warps, products per thread,
+// CTAs per SM, product values in shared memory (else in a per-CTA global slab
+// at the end of the scratch).  With the values in slabs, shared memory stops
+// limiting the resident CTAs, and more CTAs per SM hide each other's barriers.
+// Measured on the power-law workload, one bin at a time:
+//   3072: 12x8, 2 CTAs/SM, shared values    1.99 ms -> 8x12, 4 CTAs/SM, slab 1.67 ms
+//   4096: 8x16, 2 CTAs/SM, shared values    1.12 ms -> 8x16, 3 CTAs/SM, slab 1.00 ms
+//   6144: 16x12, 1 CTA/SM, shared values    1.55 ms -> 16x12, 2 CTAs/SM, slab 1.34 ms
+//   8192: 16x16, 1 CTA/SM, shared values    0.73 ms (2 CTAs/SM with a slab: the same)
+constexpr int kB13W = 8, kB13I = 12, kB13MinB = 4;
+constexpr bool kB13SV = false;
+constexpr int kB14W = 8, kB14I = 16, kB14MinB = 3;
+constexpr bool kB14SV = false;
 constexpr int kB15W = 16, kB15I = 12, kB15MinB = 2;
 constexpr bool kB15SV = false;
 constexpr int kB16W = 16, kB16I = 16, kB16MinB = 1;
 constexpr bool kB16SV = true;
 
-// Bytes of the value slabs of bins 15 and 16 (0 when their values are in
+// Bytes of the value slabs of bins 13-16 (0 for a bin whose values are in
 // shared memory).
 size_t cta_slab_bytes(int bin, int64_t count, int num_sms) {
     auto f = [&](int w, int items, int minb, bool sv) -> size_t {
@@ -396,18 +403,23 @@ size_t cta_slab_bytes(int bin, int64_t count, int num_sms) {
         const int64_t grid = std::min<int64_t>(count, static_cast<int64_t>(num_sms) * minb);
         return static_cast<size_t>(grid) * w * 32 * items * sizeof(double);
     };
-    if (bin == 15) return f(kB15W, kB15I, kB15MinB, kB15SV);
-    if (bin == 16) return f(kB16W, kB16I, kB16MinB, kB16SV);
-    return 0;
+    switch (bin) {
+        case 13: return f(kB13W, kB13I, kB13MinB, kB13SV);
+        case 14: return f(kB14W, kB14I, kB14MinB, kB14SV);
+        case 15: return f(kB15W, kB15I, kB15MinB, kB15SV);
+        case 16: return f(kB16W, kB16I, kB16MinB, kB16SV);
+        default: return 0;
+    }
 }
 
 }  // namespace
 
 size_t numeric_scratch_bytes(const int64_t* bin_count, int64_t max_ub, int num_sms, bool holes, bool concurrent) {
     // Bins 17-19 share the front of the scratch (they run one after the other);
-    // bins 15-16 take their slabs from its end, after that region when the bins
-    // run on concurrent streams.
-    const size_t cta = std::max(cta_slab_bytes(15, bin_count[15], num_sms), cta_slab_bytes(16, bin_count[16], num_sms));
+    // bins 13-16 take their slabs from its end (also one after the other), after
+    // that region when the two groups run on concurrent streams.
+    size_t cta = 0;
+    for (int b = 13; b <= 16; ++b) cta = std::max(cta, cta_slab_bytes(b, bin_count[b], num_sms));
     size_t need = 0;
     for (int b = kLastSmemBin + 1; b < kBinHeavy; ++b)  // the launches run one after the other
         if (bin_count[b])
@@ -441,12 +453,18 @@ void launch_numeric(int bin, const Job* d_jobs, const int64_t* d_items, int64_t 
     }
     double* slab = static_cast<double*>(d_scratch);
     switch (bin) {
-        case 9: run_block<3, 8, 8>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;     // <= 768
+        case 9: run_block<4, 6, 8>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;     // <= 768
         case 10: run_block<2, 16, 8>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;   // <= 1024
         case 11: run_block<6, 8, 4>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;    // <= 1536
         case 12: run_block<8, 8, 4>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;    // <= 2048
-        case 13: run_block<12, 8, 2>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;   // <= 3072
-        case 14: run_block<8, 16, 2>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;   // <= 4096
+        case 13:  // <= 3072
+            run_block<kB13W, kB13I, kB13MinB, kB13SV>(d_jobs, d_items, count, d_stats, d_err, st, num_sms,
+                                                     tail_slab(d_scratch, scratch_bytes, cta_slab_bytes(13, count, num_sms)));
+            break;
+        case 14:  // <= 4096
+            run_block<kB14W, kB14I, kB14MinB, kB14SV>(d_jobs, d_items, count, d_stats, d_err, st, num_sms,
+                                                     tail_slab(d_scratch, scratch_bytes, cta_slab_bytes(14, count, num_sms)));
+            break;
         case 15:  // <= 6144
             run_block<kB15W, kB15I, kB15MinB, kB15SV>(d_jobs, d_items, count, d_stats, d_err, st, num_sms,
                                                      tail_slab(d_scratch, scratch_bytes, cta_slab_bytes(15, count, num_sms)));

@@ -2,7 +2,7 @@
 // the autotuner (spg_tune).  Every shape runs the same per-row pipeline
 // (k_numeric_row.cuh), so results are identical; only the time differs.
 //   bins 7-8   (<= 384, <= 512 products): a 2-warp CTA per row instead of one warp
-//   bins 9-15  (<= 768 ... <= 6144):      the shapes before measurement-driven tuning
+//   bins 9-15  (<= 768 ... <= 6144):      the shapes before the last measurement-driven tuning
 #include "k_numeric_row.cuh"
 
 namespace spg {
@@ -12,7 +12,7 @@ bool launch_numeric_alt(int bin, const Job* d_jobs, const int64_t* d_items, int6
     switch (bin) {
         case 7: run_block<2, 6, 8>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); return true;    // 384
         case 8: run_block<2, 8, 8>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); return true;    // 512
-        case 9: run_block<4, 6, 6>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); return true;    // 768
+        case 9: run_block<3, 8, 8>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); return true;    // 768
         case 10: run_block<4, 8, 6>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); return true;   // 1024
         case 11: run_block<8, 6, 3>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); return true;   // 1536
         case 12: run_block<4, 16, 4>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); return true;  // 2048
