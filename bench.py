@@ -54,6 +54,7 @@ WORKLOADS = {
               "batched size distributions (<= 2M rows), device-resident operands, 150 GB admission budget",
 }
 BATCH_PRODUCTS = 512
+BATCH_MAX_PRODUCTS = 1 << 28  # scalar products per batch: ~8 ms of kernels, so the two lanes alternate
 SERVE_RATES = (50, 100, 200, 500, 1000, 2000)
 
 
@@ -487,7 +488,8 @@ def run_batched(args, rank, world, local):
             res.free()
         return nnz, batches
 
-    srv = sg.Server(local, lanes=2, max_batch=BATCH_PRODUCTS, hbm_budget_bytes=150 * 10**9)
+    srv = sg.Server(local, lanes=2, max_batch=BATCH_PRODUCTS, hbm_budget_bytes=150 * 10**9,
+                    max_batch_products=BATCH_MAX_PRODUCTS)
     for _ in range(args.warmup):
         c_nnz, _ = served(srv)
     times, waves, launches = [], [], 0
@@ -531,7 +533,8 @@ def run_batched(args, rank, world, local):
                    "rows_total": int(sum(a.rows for a, _ in pairs)), "scalar_products_per_step": int(total_p),
                    "c_nnz": int(c_nnz), "l2": f"inputs larger than L2 ({in_bytes / 1e9:.1f} GB, no flush)",
                    "timing": "host wall clock between device synchronisations (two lanes, two streams)",
-                   "server": {"lanes": 2, "max_batch": BATCH_PRODUCTS, "hbm_budget_bytes": 150 * 10**9},
+                   "server": {"lanes": 2, "max_batch": BATCH_PRODUCTS, "hbm_budget_bytes": 150 * 10**9,
+                              "max_batch_products": BATCH_MAX_PRODUCTS},
                    "waves_per_step": [len(w) for w in waves], "wave_sizes_last_step": waves[-1]},
         "per_product_launches": {"value": single, "unit": "GFLOP/s", "steps": k1,
                                  "ms_per_step": 1e3 * t_single / k1,
@@ -597,7 +600,7 @@ def _serve_trace(srv, dev, products, at, picks):
 
 def run_served(args, rank, world, local):
     """The served stream: one Poisson trace per rate, served by continuous
-    batching (3 lanes, batches of up to 256 requests / 2^29 scalar products)
+    batching (3 lanes, batches of up to 256 requests / 2^27 scalar products)
     and by per-request launches
     (1 lane, batches of 1), plus both at saturation (every request queued at
     once)."""
@@ -607,7 +610,7 @@ def run_served(args, rank, world, local):
     pool = make_workload("served")
     products = [sg.scalar_products_host(a, b) for a, b in pool]
     dev = [(a.to_device(local), b.to_device(local)) for a, b in pool]
-    modes = {"batched": dict(lanes=3, max_batch=256, max_batch_products=1 << 29),
+    modes = {"batched": dict(lanes=3, max_batch=256, max_batch_products=1 << 27),
              "per_request": dict(lanes=1, max_batch=1)}
     n_sat = 300
     table = {m: {} for m in modes}

@@ -305,8 +305,8 @@ typedef struct {
     int32_t reserved;
     uint64_t hbm_budget_bytes;  /* admission budget for in-flight work; default 150 GB */
     int64_t max_batch_products; /* a batch stops growing past this many scalar products (a lone larger
-                                   request still runs), so that a long queue splits over the lanes;
-                                   default 2^30 */
+                                   request still runs), so that a long queue splits over the lanes
+                                   and one lane's host work overlaps another's kernels; default 2^28 */
 } spg_server_config;
 
 typedef struct {

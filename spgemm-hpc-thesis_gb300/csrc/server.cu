@@ -277,7 +277,7 @@ spg_status spg_server_config_default(spg_server_config* c) {
     c->out_location = SPG_DEVICE;
     c->mode = SPG_MODE_AUTO;
     c->hbm_budget_bytes = 150ull * 1000 * 1000 * 1000;
-    c->max_batch_products = int64_t{1} << 30;
+    c->max_batch_products = int64_t{1} << 28;
     return SPG_OK;
 }
 

@@ -552,7 +552,7 @@ class Server:
     results; batches of queued requests run together on `lanes` streams."""
 
     def __init__(self, device: int = 0, lanes: int = 2, max_batch: int = 256, out: str = "device",
-                 mode: str = "auto", hbm_budget_bytes: int = 150 * 10**9, max_batch_products: int = 1 << 30):
+                 mode: str = "auto", hbm_budget_bytes: int = 150 * 10**9, max_batch_products: int = 1 << 28):
         lib = library()
         cfg = _ServerConfig(device, lanes, max_batch, SPG_DEVICE if out == "device" else SPG_HOST, MODES[mode], 0,
                             int(hbm_budget_bytes), int(max_batch_products))
