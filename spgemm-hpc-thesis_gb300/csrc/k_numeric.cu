@@ -455,7 +455,7 @@ void launch_numeric(int bin, const Job* d_jobs, const int64_t* d_items, int64_t 
     switch (bin) {
         case 9: run_block<4, 6, 8>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;     // <= 768
         case 10: run_block<2, 16, 8>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;   // <= 1024
-        case 11: run_block<6, 8, 4>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;    // <= 1536
+        case 11: run_block<8, 6, 4>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;    // <= 1536
         case 12: run_block<8, 8, 4>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;    // <= 2048
         case 13:  // <= 3072
             run_block<kB13W, kB13I, kB13MinB, kB13SV>(d_jobs, d_items, count, d_stats, d_err, st, num_sms,
