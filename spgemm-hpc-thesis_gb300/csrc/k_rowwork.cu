@@ -222,31 +222,44 @@ compact_kernel(const Job* __restrict__ job, int rows, int32_t* __restrict__ out_
 // K5 for rows written with holes (upper-bound mode): warp per row, the row's
 // reserved slots [cnt[r], cnt[r+1]) are read in order and the slots with a
 // column >= 0 are packed at the row's final offset nz[r] (ballot + popc).
+// Each warp loads its next row's offsets while it copies the current one, and
+// issues eight chunks of 32 slots per step (2.70 -> 2.45 ms on the power-law
+// workload, 89% of the measured copy bandwidth; either change alone gave < 2%).
 __global__ void __launch_bounds__(256)
 compact_holes_kernel(const Job* __restrict__ jobs, int njobs, const int64_t* __restrict__ job_row_base,
                      int64_t total_rows, int32_t* __restrict__ out_col, double* __restrict__ out_val) {
+    constexpr int kChunks = 8;
     const int lane = threadIdx.x & 31;
     const int64_t warps = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
-    for (int64_t g = static_cast<int64_t>(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5); g < total_rows;
-         g += warps) {
-        const int j = job_of_row(job_row_base, njobs, g);
+    int64_t g = static_cast<int64_t>(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    int j = 0;
+    int64_t n_src = 0, n_end = 0, n_dst = 0;
+    auto load_row = [&](int64_t row) {
+        j = job_of_row(job_row_base, njobs, row);
+        const int r = static_cast<int>(row - job_row_base[j]);
+        n_src = jobs[j].cnt[r];
+        n_end = jobs[j].cnt[r + 1];
+        n_dst = jobs[j].nz[r];
+    };
+    if (g < total_rows) load_row(g);
+    for (; g < total_rows; g += warps) {
         const Job& J = jobs[j];
-        const int r = static_cast<int>(g - job_row_base[j]);
-        const int64_t src = J.cnt[r], end = J.cnt[r + 1];
-        int64_t dst = J.nz[r];
-        // four chunks of 32 slots per step; columns and values are loaded together
-        // (a hole's value is read and dropped) so the loads do not wait on each other
-        for (int64_t q0 = src; q0 < end; q0 += 128) {
-            int32_t c[4];
-            double v[4];
+        const int64_t src = n_src, end = n_end;
+        int64_t dst = n_dst;
+        if (g + warps < total_rows) load_row(g + warps);
+        // columns and values are loaded together (a hole's value is read and
+        // dropped) so the loads do not wait on each other
+        for (int64_t q0 = src; q0 < end; q0 += kChunks * 32) {
+            int32_t c[kChunks];
+            double v[kChunks];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < kChunks; ++u) {
                 const int64_t q = q0 + u * 32 + lane;
                 c[u] = q < end ? J.c_col[q] : -1;
                 v[u] = q < end ? J.c_val[q] : 0.0;
             }
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < kChunks; ++u) {
                 const unsigned m = __ballot_sync(0xffffffffu, c[u] >= 0);
                 if (c[u] >= 0) {
                     const int64_t at = dst + __popc(m & lanemask_lt());
