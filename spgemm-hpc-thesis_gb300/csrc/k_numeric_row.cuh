@@ -24,6 +24,8 @@
 // CTA with the whole sort in a global slab (num_heavy_kernel, k_numeric.cu).
 #pragma once
 
+#include <type_traits>
+
 #include "spg_enum.cuh"
 
 namespace spg {
@@ -59,7 +61,7 @@ struct RowSmem {
     SegTab<W * 32, int32_t> seg;  // enumeration batch
     int64_t warp_tmp[W + 1];    // block scans
     uint32_t keys[kCap];        // columns (unpacked) or packed (column, sequence) words
-    uint32_t hist[W == 1 ? 1 : 2][kHistWords<W>];  // digit counters at hidx<W>(digit, warp); CTA rows
+    alignas(16) uint32_t hist[W == 1 ? 1 : 2][kHistWords<W>];  // digit counters at hidx<W>(digit, warp); CTA rows
                                                    // alternate two sets so that clearing the next
                                                    // pass's set needs no barrier of its own
     uint32_t cnt[W * ITEMS];    // kept entries per (warp, item)
@@ -69,20 +71,23 @@ struct RowSmem {
     uint32_t step_cnt[64];      // kept counts of one filtered enumeration step (row pieces)
 };
 
-// Exclusive scan of the 256*W digit counters in (digit, warp) order, 8
-// consecutive counters per thread (logical index L = d * W + w).
-template <int W>
+// Exclusive scan of the NDIG*W digit counters in (digit, warp) order (logical
+// index L = d * W + w): NDIG/32 consecutive counters per thread, one for the
+// first 16*W threads when NDIG is 16.
+template <int W, int NDIG = 256>
 __device__ inline void scan_counters(uint32_t* c, int64_t* tmp) {
-    constexpr int kPer = 8;
+    constexpr int kPer = NDIG >= 32 ? NDIG / 32 : 1;
+    constexpr int kTot = NDIG * W;
     const int lane = threadIdx.x & 31;
     const int warp = W == 1 ? 0 : (threadIdx.x >> 5);
     const int tid = W == 1 ? lane : threadIdx.x;
+    const bool act = NDIG >= 32 || tid < kTot;
     auto phys = [](int L) { return W == 1 ? L : hidx<W>(L / W, L % W); };
     uint32_t v[kPer];
     uint32_t sum = 0;
 #pragma unroll
     for (int j = 0; j < kPer; ++j) {
-        v[j] = c[phys(tid * kPer + j)];
+        v[j] = act ? c[phys(tid * kPer + j)] : 0u;
         sum += v[j];
     }
     const uint32_t incl = warp_incl_scan(sum, lane);
@@ -93,20 +98,32 @@ __device__ inline void scan_counters(uint32_t* c, int64_t* tmp) {
         const uint32_t t = lane < W ? static_cast<uint32_t>(tmp[lane]) : 0u;
         base += __shfl_sync(0xffffffffu, warp_incl_scan(t, lane) - t, warp);
     }
+    if (act) {
 #pragma unroll
-    for (int j = 0; j < kPer; ++j) {
-        c[phys(tid * kPer + j)] = base;
-        base += v[j];
+        for (int j = 0; j < kPer; ++j) {
+            c[phys(tid * kPer + j)] = base;
+            base += v[j];
+        }
     }
 }
 
-// Lanes of the warp holding the same 8-bit digit: the intersection of one
+// Zeroes the counters of the first ndig digits (ndig * kHistStride<W> words, a
+// multiple of four) with 16-byte stores; h is 16-byte aligned.
+template <int W>
+__device__ inline void clear_counters(uint32_t* h, int ndig, int tid) {
+    uint4* h4 = reinterpret_cast<uint4*>(h);
+    const int n4 = ndig * kHistStride<W> / 4;
+    for (int d = tid; d < n4; d += W * 32) h4[d] = make_uint4(0u, 0u, 0u, 0u);
+}
+
+// Lanes of the warp holding the same NB-bit digit: the intersection of one
 // ballot per digit bit (a ballot for each set bit, its complement for each
 // clear bit).  Eight votes cost a fraction of one __match_any_sync on GB300.
+template <int NB = 8>
 __device__ inline unsigned digit_peers(uint32_t d) {
     unsigned peers = 0xffffffffu;
 #pragma unroll
-    for (int b = 0; b < 8; ++b) {
+    for (int b = 0; b < NB; ++b) {
         const unsigned bit = (d >> b) & 1u;
         const unsigned set = __ballot_sync(0xffffffffu, bit);
         peers &= set ^ (bit - 1u);  // set where this lane's bit is 1, ~set where it is 0
@@ -119,8 +136,9 @@ __device__ inline unsigned digit_peers(uint32_t d) {
 // the counter by the group size (one shared atomic) and broadcasts the old
 // value.  Items of a warp are ranked in order, so ranks follow
 // (warp, item, lane) order.
+template <int NB = 8>
 __device__ inline uint32_t rank_item(uint32_t d, uint32_t* counter_of_d, int lane) {
-    const unsigned peers = digit_peers(d);
+    const unsigned peers = digit_peers<NB>(d);
     const int leader = __ffs(peers) - 1;
     uint32_t base = 0;
     if (lane == leader) base = atomicAdd(counter_of_d, static_cast<uint32_t>(__popc(peers)));
@@ -173,100 +191,99 @@ __device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double*
                            int nbits, int lane, int warp, int tid) {
     using Sm = RowSmem<W, ITEMS, SV>;
     constexpr int kSeqBits = Sm::kSeqBits;
-    // 2. stable LSD radix sort by column
+    // 2. stable LSD radix sort by column: 8-bit digits, and a last pass of at
+    //    most 4 bits (four votes, 16 counters per warp) when no more remain
     int hb = 0;  // counter set of this pass
-    auto clear_next = [&](int set) {
-        for (int d = tid; d < kHistWords<W>; d += W * 32) sm.hist[set][d] = 0;
-    };
-    clear_next(0);
-    row_sync<W>();
+    auto digits_from = [&](int shift) { return nbits - shift > 4 ? 256 : 16; };
     if constexpr (PACKED) {
-        // Packed words (col - cmin) << kSeqBits | seq; the first pass packs.
-        for (int shift = 0; shift < nbits || shift == 0; shift += 8) {
-            uint32_t k[ITEMS], rk[ITEMS];
-            uint32_t* hist = sm.hist[hb];
+        if (nbits == 0) {  // one column: already in sequence order; just pack
 #pragma unroll
             for (int i = 0; i < ITEMS; ++i) {
                 const int pos = (warp * ITEMS + i) * 32 + lane;
-                uint32_t d = 255u;
+                if (pos < P) sm.keys[pos] = ((sm.keys[pos] - cmin) << kSeqBits) | static_cast<uint32_t>(pos);
+            }
+        }
+    } else {
+        for (int i = tid; i < P; i += W * 32) sm.seqs[i] = static_cast<uint16_t>(i);
+    }
+    if (nbits > 0) clear_counters<W>(sm.hist[0], digits_from(0), tid);
+    row_sync<W>();
+    // One pass over the digit of NB bits at `shift` (NB = 8, or 4 for the last).
+    auto pass = [&](auto nb, int shift) {
+        constexpr int NB = decltype(nb)::value;
+        constexpr uint32_t kMask = (1u << NB) - 1u;
+        uint32_t* hist = sm.hist[hb];
+        uint32_t k[ITEMS], rk[ITEMS];
+        if constexpr (PACKED) {
+            // Packed words (col - cmin) << kSeqBits | seq; the first pass packs.
+#pragma unroll
+            for (int i = 0; i < ITEMS; ++i) {
+                const int pos = (warp * ITEMS + i) * 32 + lane;
+                uint32_t d = kMask;
                 k[i] = 0xffffffffu;
                 if (pos < P) {
                     const uint32_t raw = sm.keys[pos];
                     k[i] = shift == 0 ? ((raw - cmin) << kSeqBits) | static_cast<uint32_t>(pos) : raw;
-                    d = (k[i] >> (kSeqBits + shift)) & 255u;
+                    d = (k[i] >> (kSeqBits + shift)) & kMask;
                 }
-                rk[i] = rank_item(d, &hist[hidx<W>(d, warp)], lane);
-            }
-            if (nbits == 0) {  // one column: already in sequence order; just pack
-                row_sync<W>();
-#pragma unroll
-                for (int i = 0; i < ITEMS; ++i) {
-                    const int pos = (warp * ITEMS + i) * 32 + lane;
-                    if (pos < P) sm.keys[pos] = k[i];
-                }
-                row_sync<W>();
-                break;
+                rk[i] = rank_item<NB>(d, &hist[hidx<W>(d, warp)], lane);
             }
             row_sync<W>();
-            scan_counters<W>(hist, sm.warp_tmp);
+            scan_counters<W, (1 << NB)>(hist, sm.warp_tmp);
             row_sync<W>();
 #pragma unroll
             for (int i = 0; i < ITEMS; ++i) {
-                // Padding items were ranked under digit 255; a recomputed digit of
-                // 0xffffffff is not 255 once fewer than 8 key bits remain.
+                // Padding items were ranked under the largest digit, after every
+                // real item of that digit; they are not stored.
                 const int pos = (warp * ITEMS + i) * 32 + lane;
                 if (pos < P) {
-                    const uint32_t d = (k[i] >> (kSeqBits + shift)) & 255u;
+                    const uint32_t d = (k[i] >> (kSeqBits + shift)) & kMask;
                     sm.keys[hist[hidx<W>(d, warp)] + rk[i]] = k[i];
                 }
             }
-            if constexpr (W == 1) {
-                __syncwarp();
-                clear_next(0);
-            } else {
-                clear_next(hb ^ 1);
-                hb ^= 1;
-            }
-            row_sync<W>();
-        }
-    } else {
-        for (int i = tid; i < P; i += W * 32) sm.seqs[i] = static_cast<uint16_t>(i);
-        row_sync<W>();
-        for (int shift = 0; shift < nbits; shift += 8) {
-            uint32_t k[ITEMS], rk[ITEMS];
-            uint16_t s[ITEMS];
-            uint32_t* hist = sm.hist[hb];
+        } else {
+            uint16_t sq[ITEMS];
 #pragma unroll
             for (int i = 0; i < ITEMS; ++i) {
                 const int pos = (warp * ITEMS + i) * 32 + lane;
                 const bool valid = pos < P;
                 k[i] = valid ? sm.keys[pos] : 0u;
-                s[i] = valid ? sm.seqs[pos] : uint16_t{0};
-                const uint32_t d = valid ? (((k[i] - cmin) >> shift) & 255u) : 255u;
-                rk[i] = rank_item(d, &hist[hidx<W>(d, warp)], lane);
+                sq[i] = valid ? sm.seqs[pos] : uint16_t{0};
+                const uint32_t d = valid ? (((k[i] - cmin) >> shift) & kMask) : kMask;
+                rk[i] = rank_item<NB>(d, &hist[hidx<W>(d, warp)], lane);
             }
             row_sync<W>();
-            scan_counters<W>(hist, sm.warp_tmp);
+            scan_counters<W, (1 << NB)>(hist, sm.warp_tmp);
             row_sync<W>();
 #pragma unroll
             for (int i = 0; i < ITEMS; ++i) {
                 const int pos = (warp * ITEMS + i) * 32 + lane;
-                const uint32_t d = pos < P ? (((k[i] - cmin) >> shift) & 255u) : 255u;
+                const uint32_t d = pos < P ? (((k[i] - cmin) >> shift) & kMask) : kMask;
                 const uint32_t dst = hist[hidx<W>(d, warp)] + rk[i];
                 if (dst < static_cast<uint32_t>(P)) {
                     sm.keys[dst] = k[i];
-                    sm.seqs[dst] = s[i];
+                    sm.seqs[dst] = sq[i];
                 }
             }
-            if constexpr (W == 1) {
-                __syncwarp();
-                clear_next(0);
-            } else {
-                clear_next(hb ^ 1);
-                hb ^= 1;
-            }
-            row_sync<W>();
         }
+    };
+    for (int shift = 0; shift < nbits;) {
+        if (nbits - shift > 4) {
+            pass(std::integral_constant<int, 8>{}, shift);
+            shift += 8;
+        } else {
+            pass(std::integral_constant<int, 4>{}, shift);
+            shift += 4;
+        }
+        const bool more = shift < nbits;
+        if constexpr (W == 1) {
+            __syncwarp();
+            if (more) clear_counters<W>(sm.hist[0], digits_from(shift), tid);
+        } else {
+            if (more) clear_counters<W>(sm.hist[hb ^ 1], digits_from(shift), tid);
+            hb ^= 1;
+        }
+        row_sync<W>();
     }
 
     // Column and sequence number of sorted position pos.
