@@ -53,6 +53,39 @@ def test_every_bin(engine, port, seed):
     assert all(t["bin_rows"][name] >= 1 for name in BIN_NAMES), t["bin_rows"]
 
 
+def column_window_case(width: int, seed: int):
+    """(A, B) whose every output row spans exactly 2**width columns (the window
+    [base, base + 2**width - 1], both ends in every B row), with rows of 0, 40,
+    200, 500, 1,200, 3,000 and 15,000 scalar products (warp-row bins, CTA
+    bins with shared and global value slabs, the 16K bin)."""
+    rng = np.random.default_rng(seed)
+    base = 1000
+    lo, hi = base, base + (1 << width) - 1
+    inner, blen = 200, 20
+    cols = rng.integers(lo, hi + 1, size=(inner, blen), dtype=np.int64)
+    cols[:, 0], cols[:, 1] = lo, hi
+    for r in range(inner):
+        rng.shuffle(cols[r])
+    b = Csr(inner, hi + 7, np.arange(inner + 1, dtype=np.int64) * blen, cols.reshape(-1).astype(np.int32),
+            rng.uniform(-1, 1, size=inner * blen))
+    counts = [0, 2, 10, 25, 60, 150, 750]  # A entries per row: products = 20 x count
+    rp = np.zeros(len(counts) + 1, dtype=np.int64)
+    rp[1:] = np.cumsum(counts)
+    a = Csr(len(counts), inner, rp, rng.integers(0, inner, size=int(rp[-1])).astype(np.int32),
+            rng.uniform(-1, 1, size=int(rp[-1])))
+    return a, b
+
+
+@pytest.mark.parametrize("width", [0, 1, 3, 4, 5, 8, 9, 12, 13, 16, 17, 19, 20, 21, 24, 25])
+def test_column_range_widths(engine, port, width):
+    # The radix sort takes 8-bit passes and a last pass of at most 4 bits, over
+    # the bits of max(col) - min(col) only; keys pack (column, sequence) into
+    # 32 bits unless the width and the sequence bits exceed that (widths >= 19
+    # in the 16K bin, >= 21 in the 3K bin, >= 25 in the warp bins).
+    a, b = column_window_case(width, 40 + width)
+    check(engine, port, a, b)
+
+
 def test_known_answer(engine):
     # spgemm_serial_smoke.cpp:65-67
     a = Csr.from_arrays(2, 3, [0, 2, 3], [0, 2, 1], [1.0, 2.0, 3.0])
