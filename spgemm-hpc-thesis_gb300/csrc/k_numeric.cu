@@ -377,15 +377,23 @@ int heavy_grid(int64_t count, int num_sms) { return static_cast<int>(count < num
 // Product-value slab of one CTA of the two global-slab bins.
 constexpr int64_t slab_cap(int bin) { return bin == 17 ? 16 * 32 * 24 : 16 * 32 * 32; }
 
-// Team shapes of the bins of 2049-8192 products: warps, products per thread,
-// CTAs per SM, product values in shared memory (else in a per-CTA global slab
-// at the end of the scratch).  With the values in slabs, shared memory stops
-// limiting the resident CTAs, and more CTAs per SM hide each other's barriers.
-// Measured on the power-law workload, one bin at a time:
+// Team shapes of the bins of 769-1024 and 2049-8192 products: warps, products
+// per thread, CTAs per SM, product values in shared memory (else in a per-CTA
+// global slab at the end of the scratch).  With the values in slabs, shared
+// memory stops limiting the resident CTAs, and more CTAs per SM hide each
+// other's barriers.  Measured on the power-law workload, one bin at a time:
+//   1024: 2x16, 8 CTAs/SM, shared values    1.48 ms -> 2x16, 12 CTAs/SM, slab 1.34 ms
+//         (9 CTAs/SM with shared values 1.56 ms, 10 with a slab 1.46 ms)
 //   3072: 12x8, 2 CTAs/SM, shared values    1.99 ms -> 8x12, 4 CTAs/SM, slab 1.67 ms
 //   4096: 8x16, 2 CTAs/SM, shared values    1.12 ms -> 8x16, 3 CTAs/SM, slab 1.00 ms
+//         (8x16 at 4 CTAs/SM with a slab 0.97 ms, 16x8 at 2 1.02 ms)
 //   6144: 16x12, 1 CTA/SM, shared values    1.55 ms -> 16x12, 2 CTAs/SM, slab 1.34 ms
+//         (8x24 at 3 CTAs/SM 1.42 ms, 12x16 at 2 1.33 ms against 1.28)
 //   8192: 16x16, 1 CTA/SM, shared values    0.73 ms (2 CTAs/SM with a slab: the same)
+// The slabs of these bins share one region: the bins run one after the other
+// on one stream.
+constexpr int kB10W = 2, kB10I = 16, kB10MinB = 12;
+constexpr bool kB10SV = false;
 constexpr int kB13W = 8, kB13I = 12, kB13MinB = 4;
 constexpr bool kB13SV = false;
 constexpr int kB14W = 8, kB14I = 16, kB14MinB = 3;
@@ -395,8 +403,8 @@ constexpr bool kB15SV = false;
 constexpr int kB16W = 16, kB16I = 16, kB16MinB = 1;
 constexpr bool kB16SV = true;
 
-// Bytes of the value slabs of bins 13-16 (0 for a bin whose values are in
-// shared memory).
+// Bytes of the value slabs of bins 10 and 13-16 (0 for a bin whose values are
+// in shared memory).
 size_t cta_slab_bytes(int bin, int64_t count, int num_sms) {
     auto f = [&](int w, int items, int minb, bool sv) -> size_t {
         if (sv || count <= 0) return 0;
@@ -404,6 +412,7 @@ size_t cta_slab_bytes(int bin, int64_t count, int num_sms) {
         return static_cast<size_t>(grid) * w * 32 * items * sizeof(double);
     };
     switch (bin) {
+        case 10: return f(kB10W, kB10I, kB10MinB, kB10SV);
         case 13: return f(kB13W, kB13I, kB13MinB, kB13SV);
         case 14: return f(kB14W, kB14I, kB14MinB, kB14SV);
         case 15: return f(kB15W, kB15I, kB15MinB, kB15SV);
@@ -416,9 +425,9 @@ size_t cta_slab_bytes(int bin, int64_t count, int num_sms) {
 
 size_t numeric_scratch_bytes(const int64_t* bin_count, int64_t max_ub, int num_sms, bool holes, bool concurrent) {
     // Bins 17-19 share the front of the scratch (they run one after the other);
-    // bins 13-16 take their slabs from its end (also one after the other), after
-    // that region when the two groups run on concurrent streams.
-    size_t cta = 0;
+    // bins 10 and 13-16 take their slabs from its end (also one after the
+    // other), after that region when the two groups run on concurrent streams.
+    size_t cta = cta_slab_bytes(10, bin_count[10], num_sms);
     for (int b = 13; b <= 16; ++b) cta = std::max(cta, cta_slab_bytes(b, bin_count[b], num_sms));
     size_t need = 0;
     for (int b = kLastSmemBin + 1; b < kBinHeavy; ++b)  // the launches run one after the other
@@ -454,7 +463,10 @@ void launch_numeric(int bin, const Job* d_jobs, const int64_t* d_items, int64_t 
     double* slab = static_cast<double*>(d_scratch);
     switch (bin) {
         case 9: run_block<4, 6, 8>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;     // <= 768
-        case 10: run_block<2, 16, 8>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;   // <= 1024
+        case 10:  // <= 1024
+            run_block<kB10W, kB10I, kB10MinB, kB10SV>(d_jobs, d_items, count, d_stats, d_err, st, num_sms,
+                                                     tail_slab(d_scratch, scratch_bytes, cta_slab_bytes(10, count, num_sms)));
+            break;
         case 11: run_block<8, 6, 4>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;    // <= 1536
         case 12: run_block<8, 8, 4>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;    // <= 2048
         case 13:  // <= 3072
