@@ -335,11 +335,14 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
     // of its product count (ub) and compacted afterwards; in the exact mode a
     // symbolic phase counts the distinct columns of every row first.
     const bool exact = use_exact_mode(h, products, ar.bytes());
-    size_t scratch_bytes = numeric_scratch_bytes(bin_count, max_ub, h->num_sms, !exact);
+    const SplitTotals split = split_totals(hc->stats);
+    size_t scratch_bytes = numeric_scratch_bytes(bin_count, max_ub, split, h->num_sms, !exact);
     if (exact) scratch_bytes = std::max(scratch_bytes, symbolic_scratch_bytes(bin_count, max_ub, h->num_sms));
     void* scratch = scratch_bytes ? ar.alloc<unsigned char>(scratch_bytes, "heavy scratch") : nullptr;
     int64_t* partials = ar.alloc<int64_t>(scan_partials_count(static_cast<int64_t>(slots)), "scan partials");
-    for (int b = 1; b < kNumBins; ++b) launches += bin_count[b] > 0 ? (exact ? 2 : 1) : 0;
+    // K2 and K4 per bin; in the upper-bound layout the split rows take three
+    // K4 launches (planner, pieces, global-slab rows)
+    for (int b = 1; b < kNumBins; ++b) launches += bin_count[b] > 0 ? (exact ? 2 : (b > kLastSmemBin ? 3 : 1)) : 0;
     launches += 3;  // scan
     int64_t tmp_total = products;
     // The bins of K2 and K4 run on three streams (warp bins; shared-memory CTA
@@ -406,8 +409,8 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
         const int b = one_stream ? i : kNumBins - i;
         if (!bin_count[b]) continue;
         cudaStream_t bs = stream_of(b);
-        launch_numeric(b, d_jobs, items + bin_off[b], bin_count[b], max_ub, scratch, scratch_bytes, &d_ctrl->stats,
-                       &d_ctrl->err, bs, h->num_sms, !exact, h->bin_variant[b]);
+        launch_numeric(b, d_jobs, items + bin_off[b], bin_count[b], max_ub, split, scratch, scratch_bytes,
+                       &d_ctrl->stats, &d_ctrl->err, bs, h->num_sms, !exact, h->bin_variant[b]);
         cudaEventRecord(h->bin_ev[b], bs);
     }
     join();
@@ -1296,7 +1299,8 @@ void plan_build(spg_plan* p, int32_t n, const spg_csr_view* A, const spg_csr_vie
         jobs[j].c_val = tmp_val;
     }
     check_cuda(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(Job) * n, cudaMemcpyHostToDevice, st), "H2D");
-    const size_t scratch_bytes = numeric_scratch_bytes(bin_count, max_ub, h->num_sms, true);
+    const SplitTotals split = split_totals(p->hc->stats);
+    const size_t scratch_bytes = numeric_scratch_bytes(bin_count, max_ub, split, h->num_sms, true);
     void* scratch = scratch_bytes ? plan_alloc<unsigned char>(p, scratch_bytes, "plan scratch") : nullptr;
     p->col = plan_alloc<int32_t>(p, static_cast<size_t>(products), "plan C col");
     p->val = plan_alloc<double>(p, static_cast<size_t>(products), "plan C val");
@@ -1319,7 +1323,7 @@ void plan_build(spg_plan* p, int32_t n, const spg_csr_view* A, const spg_csr_vie
     for (cudaStream_t a : h->aux) cudaStreamWaitEvent(a, h->fork, 0);
     for (int b = kNumBins - 1; b >= 1; --b)
         if (bin_count[b])
-            launch_numeric(b, d_jobs, items + bin_off[b], bin_count[b], max_ub, scratch, scratch_bytes,
+            launch_numeric(b, d_jobs, items + bin_off[b], bin_count[b], max_ub, split, scratch, scratch_bytes,
                            &d_ctrl->stats, &d_ctrl->err,
                            b <= kLastWarpBin ? st : (b <= kLastSmemBin ? h->aux[0] : h->aux[1]), h->num_sms, true,
                            h->bin_variant[b]);

@@ -220,27 +220,38 @@ num_heavy_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items
 }
 
 // ---------------------------------------------------------------------------
-// Heavy rows in upper-bound mode: split by column range into pieces of at
-// most kPieceCap products, which run on the CTA pipeline of the 16384-product
-// bin (keys in shared memory, values in a global slab), many pieces of one row
-// in parallel.  The planner histograms the row's product columns into
-// kPlanBuckets buckets of the column space and cuts greedily: each piece takes
-// the longest run of buckets that still fits kPieceCap (a binary search over
-// the bucket prefixes).  Rows with a bucket above kPieceCap or more than
-// kMaxPieces pieces keep the global-slab path.  A piece owns the slots of its
-// products in the row's reserved range (the products of earlier pieces have
-// smaller columns, so they sort first).
+// Rows of more than kSplitThreshold products in upper-bound mode: split by
+// column range into pieces of at most kPieceCap products, which run on the CTA
+// pipeline of the 4096-product bin (8 warps x 16 products, values in a global
+// slab, 3 CTAs per SM), many pieces of one row in parallel.  Those rows' own
+// CTA kernels keep one 16-warp CTA per SM and leave most issue slots idle
+// (25% of the warps resident); the pieces run at the occupancy of the CTA bins.
+//
+// split_plan_kernel, one CTA per row: enumerates the row once, stages every
+// product (column, a*b) in product order in scratch and histograms the columns
+// into kPlanBuckets buckets of the column space; then cuts greedily: each
+// piece takes the longest run of buckets that still fits kPieceCap (a binary
+// search over the bucket prefixes).  Rows with a bucket above kPieceCap or
+// more than kMaxPieces pieces keep the global-slab path (num_heavy_kernel).  A
+// piece owns the slots of its products in the row's reserved range (the
+// products of earlier pieces have smaller columns, so they sort first).
+// num_piece_kernel: each piece collects its range from the row's staging in
+// product order (staged_products_in), then sorts, sums and writes like a row.
 constexpr int kPlanThreads = 512;
 constexpr int kPlanBuckets = 4096;
-constexpr uint32_t kPieceCap = 16383;
+constexpr uint32_t kPieceCap = 4096;
 constexpr int kMaxPieces = 256;
-constexpr int kPieceW = 16, kPieceItems = 32;
+constexpr int kPieceW = 8, kPieceItems = 16, kPieceMinB = 3;
+static_assert(kPieceW * 32 * kPieceItems >= static_cast<int>(kPieceCap), "a piece fits the CTA pipeline");
 
-struct HeavyPlan {
-    unsigned long long* counters;  // [0] pieces, [1] rows left to the global-slab path
+struct SplitPlan {
+    unsigned long long* counters;  // [0] pieces, [1] rows left to the global-slab path, [2] staged products
     Piece* pieces;
     int64_t* fallback;
     int64_t max_pieces;
+    int32_t* stage_col;  // staged products of the split rows (columns, values)
+    double* stage_val;
+    int64_t stage_cap;
 };
 
 struct PlanSmem {
@@ -251,10 +262,11 @@ struct PlanSmem {
     uint32_t maxc;
     int32_t npieces;
     unsigned long long base;
+    unsigned long long stage;
 };
 
 __global__ void __launch_bounds__(kPlanThreads)
-heavy_plan_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items, int64_t count, HeavyPlan plan,
+split_plan_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items, int64_t count, SplitPlan plan,
                   ErrWord* __restrict__ err) {
     __shared__ PlanSmem sm;
     constexpr int kPer = kPlanBuckets / kPlanThreads;
@@ -264,15 +276,30 @@ heavy_plan_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ item
         const Job& J = jobs[item_job(it)];
         const int row = item_row(it);
         const int32_t ncols = J.B.cols;
+        const int64_t P = J.ub[row];
         const int shift = max(0, ceil_log2(max(ncols, 1)) - 12);  // 4096 << shift >= ncols
         for (int k = tid; k < kPlanBuckets; k += kPlanThreads) sm.bucket[k] = 0;
-        if (tid == 0) sm.maxc = 0;
+        if (tid == 0) {
+            sm.maxc = 0;
+            sm.stage = atomicAdd(plan.counters + 2, static_cast<unsigned long long>(P));
+        }
         __syncthreads();
-        team_products<kPlanThreads, false, int32_t>(J, row, sm.seg, sm.warp_tmp, tid,
-                                                    [&](int32_t, int32_t c, double, double) {
-                                                        if (c < 0 || c >= ncols) c = 0;
-                                                        atomicAdd(&sm.bucket[c >> shift], 1u);
-                                                    });
+        const bool staged = sm.stage + static_cast<unsigned long long>(P) <= static_cast<unsigned long long>(plan.stage_cap);
+        if (!staged && tid == 0) raise_error(err, kErrOverflow, 9, row);
+        int32_t* scol = plan.stage_col + (staged ? sm.stage : 0);
+        double* sval = plan.stage_val + (staged ? sm.stage : 0);
+        team_products<kPlanThreads, true, int32_t>(J, row, sm.seg, sm.warp_tmp, tid,
+                                                   [&](int32_t seq, int32_t c, double b, double a) {
+                                                       if (c < 0 || c >= ncols) {
+                                                           raise_error(err, kErrInvalid, 4, c);
+                                                           c = 0;
+                                                       }
+                                                       atomicAdd(&sm.bucket[c >> shift], 1u);
+                                                       if (staged && seq < P) {
+                                                           scol[seq] = c;
+                                                           sval[seq] = __dmul_rn(a, b);
+                                                       }
+                                                   });
         uint32_t v[kPer];
         uint32_t sum = 0, mx = 0;
 #pragma unroll
@@ -290,12 +317,12 @@ heavy_plan_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ item
             run += v[j];
         }
         __syncthreads();
-        const uint32_t total = static_cast<uint32_t>(J.ub[row]);
+        const uint32_t total = static_cast<uint32_t>(P);
         if (tid == 0) {
             // greedy cut: prefix(e) = sm.bucket[e] (exclusive) for e < kPlanBuckets, total at the end
             auto prefix = [&](int e) { return e < kPlanBuckets ? sm.bucket[e] : total; };
             int np = 0, k = 0;
-            bool ok = sm.maxc <= kPieceCap;
+            bool ok = staged && sm.maxc <= kPieceCap;
             while (ok && k < kPlanBuckets) {
                 if (np == kMaxPieces) {
                     ok = false;
@@ -330,17 +357,20 @@ heavy_plan_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ item
             pc.hi = k1 < kPlanBuckets ? (k1 << shift) : INT32_MAX;
             pc.slot_off = sm.bucket[k0];
             pc.count = static_cast<int64_t>(k1 < kPlanBuckets ? sm.bucket[k1] : total) - pc.slot_off;
+            pc.scol = scol;
+            pc.sval = sval;
             plan.pieces[sm.base + tid] = pc;
         }
         __syncthreads();
     }
 }
 
-__global__ void __launch_bounds__(kPieceW * 32, 1)
-num_piece_kernel(const Job* __restrict__ jobs, HeavyPlan plan, Stats* __restrict__ stats, ErrWord* __restrict__ err,
+template <int W, int ITEMS, int MINB>
+__global__ void __launch_bounds__(W * 32, MINB)
+num_piece_kernel(const Job* __restrict__ jobs, SplitPlan plan, Stats* __restrict__ stats, ErrWord* __restrict__ err,
                  double* __restrict__ gvals) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    using Sm = RowSmem<kPieceW, kPieceItems, false>;
+    using Sm = RowSmem<W, ITEMS, false>;
     Sm& sm = *reinterpret_cast<Sm*>(smem_raw);
     double* vals = gvals + static_cast<size_t>(blockIdx.x) * Sm::kCap;
     const int64_t count = min(static_cast<int64_t>(*plan.counters), plan.max_pieces);
@@ -349,26 +379,39 @@ num_piece_kernel(const Job* __restrict__ jobs, HeavyPlan plan, Stats* __restrict
         const Piece pc = plan.pieces[i];
         if (pc.count <= 0) continue;  // an empty last piece (same for the whole CTA)
         const Job& J = jobs[item_job(pc.item)];
-        numeric_row<kPieceW, kPieceItems, false, true>(J, item_row(pc.item), sm, vals, err, &pc);
+        numeric_row<W, ITEMS, false, true>(J, item_row(pc.item), sm, vals, err, &pc);
         if (threadIdx.x == 0) mine += sm.kept;
     }
     if (threadIdx.x == 0 && mine) atomicAdd(&stats->nz_total, mine);
 }
 
-// Scratch layout of the heavy bin in upper-bound mode.
-struct HeavyLayout {
-    size_t pieces_off, fallback_off, slab_off, bytes;
+// Scratch layout of the split rows (upper-bound mode): counters | pieces |
+// fallback rows | staged columns | staged values | slabs (the pieces' value
+// slabs, then the global-slab sort of the fallback rows: one after the other).
+struct SplitLayout {
+    size_t pieces_off, fallback_off, col_off, val_off, slab_off, bytes;
     int64_t max_pieces;
 };
 
-HeavyLayout heavy_layout(int64_t count, int64_t max_ub, size_t slab_bytes) {
-    HeavyLayout L;
-    L.max_pieces = count * (2 * (max_ub / kPieceCap) + 4);  // two neighbouring greedy pieces exceed the cap
+int heavy_grid(int64_t count, int num_sms);
+
+// Depends only on the call's totals, so that the launches of bins 17-19 (one
+// after the other on one stream) lay the same scratch out identically.
+SplitLayout split_layout(int64_t max_ub, const SplitTotals& split, int num_sms) {
+    SplitLayout L;
+    const int64_t rows = split.rows, split_products = split.products;
+    // two neighbouring greedy pieces of a row together exceed the cap: at most
+    // 2 * ub / cap + 1 pieces per row
+    L.max_pieces = 2 * split_products / kPieceCap + rows;
     auto up = [](size_t x) { return (x + 255) & ~size_t{255}; };
     L.pieces_off = 256;
     L.fallback_off = up(L.pieces_off + static_cast<size_t>(L.max_pieces) * sizeof(Piece));
-    L.slab_off = up(L.fallback_off + static_cast<size_t>(count) * sizeof(int64_t));
-    L.bytes = L.slab_off + slab_bytes;
+    L.col_off = up(L.fallback_off + static_cast<size_t>(rows) * sizeof(int64_t));
+    L.val_off = up(L.col_off + static_cast<size_t>(split_products) * sizeof(int32_t));
+    L.slab_off = up(L.val_off + static_cast<size_t>(split_products) * sizeof(double));
+    const size_t piece_slab = static_cast<size_t>(num_sms) * kPieceMinB * kPieceW * 32 * kPieceItems * sizeof(double);
+    const size_t global_slab = static_cast<size_t>(heavy_grid(rows, num_sms)) * 24 * static_cast<size_t>(max_ub);
+    L.bytes = L.slab_off + std::max(piece_slab, global_slab);
     return L;
 }
 
@@ -377,13 +420,15 @@ int heavy_grid(int64_t count, int num_sms) { return static_cast<int>(count < num
 // Product-value slab of one CTA of the two global-slab bins.
 constexpr int64_t slab_cap(int bin) { return bin == 17 ? 16 * 32 * 24 : 16 * 32 * 32; }
 
-// Team shapes of the bins of 769-1024 and 2049-8192 products: warps, products
+// Team shapes of the bins of 769-1536 and 2049-8192 products: warps, products
 // per thread, CTAs per SM, product values in shared memory (else in a per-CTA
 // global slab at the end of the scratch).  With the values in slabs, shared
 // memory stops limiting the resident CTAs, and more CTAs per SM hide each
 // other's barriers.  Measured on the power-law workload, one bin at a time:
 //   1024: 2x16, 8 CTAs/SM, shared values    1.48 ms -> 2x16, 12 CTAs/SM, slab 1.34 ms
 //         (9 CTAs/SM with shared values 1.56 ms, 10 with a slab 1.46 ms)
+//   1536: 8x6, 4 CTAs/SM, shared values     1.99 ms -> 4x12, 8 CTAs/SM, slab 1.90 ms
+//         (8x6 at 5 CTAs/SM with a slab 2.02 ms)
 //   3072: 12x8, 2 CTAs/SM, shared values    1.99 ms -> 8x12, 4 CTAs/SM, slab 1.67 ms
 //   4096: 8x16, 2 CTAs/SM, shared values    1.12 ms -> 8x16, 3 CTAs/SM, slab 1.00 ms
 //         (8x16 at 4 CTAs/SM with a slab 0.97 ms, 16x8 at 2 1.02 ms)
@@ -394,6 +439,8 @@ constexpr int64_t slab_cap(int bin) { return bin == 17 ? 16 * 32 * 24 : 16 * 32 
 // on one stream.
 constexpr int kB10W = 2, kB10I = 16, kB10MinB = 12;
 constexpr bool kB10SV = false;
+constexpr int kB11W = 4, kB11I = 12, kB11MinB = 8;
+constexpr bool kB11SV = false;
 constexpr int kB13W = 8, kB13I = 12, kB13MinB = 4;
 constexpr bool kB13SV = false;
 constexpr int kB14W = 8, kB14I = 16, kB14MinB = 3;
@@ -403,8 +450,8 @@ constexpr bool kB15SV = false;
 constexpr int kB16W = 16, kB16I = 16, kB16MinB = 1;
 constexpr bool kB16SV = true;
 
-// Bytes of the value slabs of bins 10 and 13-16 (0 for a bin whose values are
-// in shared memory).
+// Bytes of the value slabs of bins 10, 11 and 13-16 (0 for a bin whose values
+// are in shared memory).
 size_t cta_slab_bytes(int bin, int64_t count, int num_sms) {
     auto f = [&](int w, int items, int minb, bool sv) -> size_t {
         if (sv || count <= 0) return 0;
@@ -413,6 +460,7 @@ size_t cta_slab_bytes(int bin, int64_t count, int num_sms) {
     };
     switch (bin) {
         case 10: return f(kB10W, kB10I, kB10MinB, kB10SV);
+        case 11: return f(kB11W, kB11I, kB11MinB, kB11SV);
         case 13: return f(kB13W, kB13I, kB13MinB, kB13SV);
         case 14: return f(kB14W, kB14I, kB14MinB, kB14SV);
         case 15: return f(kB15W, kB15I, kB15MinB, kB15SV);
@@ -423,25 +471,23 @@ size_t cta_slab_bytes(int bin, int64_t count, int num_sms) {
 
 }  // namespace
 
-size_t numeric_scratch_bytes(const int64_t* bin_count, int64_t max_ub, int num_sms, bool holes, bool concurrent) {
+size_t numeric_scratch_bytes(const int64_t* bin_count, int64_t max_ub, const SplitTotals& split, int num_sms,
+                             bool holes, bool concurrent) {
     // Bins 17-19 share the front of the scratch (they run one after the other);
-    // bins 10 and 13-16 take their slabs from its end (also one after the
+    // bins 10, 11 and 13-16 take their slabs from its end (also one after the
     // other), after that region when the two groups run on concurrent streams.
-    size_t cta = cta_slab_bytes(10, bin_count[10], num_sms);
-    for (int b = 13; b <= 16; ++b) cta = std::max(cta, cta_slab_bytes(b, bin_count[b], num_sms));
+    size_t cta = 0;
+    for (int b = 10; b <= 16; ++b) cta = std::max(cta, cta_slab_bytes(b, bin_count[b], num_sms));
     size_t need = 0;
-    for (int b = kLastSmemBin + 1; b < kBinHeavy; ++b)  // the launches run one after the other
-        if (bin_count[b])
-            need = std::max(need, static_cast<size_t>(slab_grid(bin_count[b], num_sms)) * slab_cap(b) * sizeof(double));
-    const int64_t heavy = bin_count[kBinHeavy];
-    if (heavy) {
-        const size_t global_slab = static_cast<size_t>(heavy_grid(heavy, num_sms)) * 24 * static_cast<size_t>(max_ub);
-        if (holes) {
-            const size_t piece_slab = static_cast<size_t>(num_sms) * kPieceW * 32 * kPieceItems * sizeof(double);
-            need = std::max(need, heavy_layout(heavy, max_ub, std::max(global_slab, piece_slab)).bytes);
-        } else {
-            need = std::max(need, global_slab);
-        }
+    if (holes) {
+        if (split.rows > 0) need = split_layout(max_ub, split, num_sms).bytes;
+    } else {
+        for (int b = kLastSmemBin + 1; b < kBinHeavy; ++b)  // the launches run one after the other
+            if (bin_count[b])
+                need = std::max(need, static_cast<size_t>(slab_grid(bin_count[b], num_sms)) * slab_cap(b) * sizeof(double));
+        const int64_t heavy = bin_count[kBinHeavy];
+        if (heavy)
+            need = std::max(need, static_cast<size_t>(heavy_grid(heavy, num_sms)) * 24 * static_cast<size_t>(max_ub));
     }
     return concurrent ? ((need + 255) & ~size_t{255}) + cta : std::max(need, cta);
 }
@@ -451,13 +497,45 @@ static double* tail_slab(void* d_scratch, size_t scratch_bytes, size_t need) {
     return need ? reinterpret_cast<double*>(static_cast<unsigned char*>(d_scratch) + (scratch_bytes - need)) : nullptr;
 }
 
+// Rows of more than kSplitThreshold products in upper-bound mode: plan and
+// stage, the pieces, then the rows left to the global-slab sort.
+static void launch_split(const Job* d_jobs, const int64_t* d_items, int64_t count, int64_t max_ub,
+                         const SplitTotals& split, void* d_scratch, Stats* d_stats, ErrWord* d_err, cudaStream_t st,
+                         int num_sms) {
+    const SplitLayout L = split_layout(max_ub, split, num_sms);
+    unsigned char* base = static_cast<unsigned char*>(d_scratch);
+    SplitPlan plan;
+    plan.counters = reinterpret_cast<unsigned long long*>(base);
+    plan.pieces = reinterpret_cast<Piece*>(base + L.pieces_off);
+    plan.fallback = reinterpret_cast<int64_t*>(base + L.fallback_off);
+    plan.max_pieces = L.max_pieces;
+    plan.stage_col = reinterpret_cast<int32_t*>(base + L.col_off);
+    plan.stage_val = reinterpret_cast<double*>(base + L.val_off);
+    plan.stage_cap = split.products;
+    void* slabs = base + L.slab_off;
+    cudaMemsetAsync(plan.counters, 0, 4 * sizeof(unsigned long long), st);
+    split_plan_kernel<<<static_cast<int>(std::min<int64_t>(count, 3 * num_sms)), kPlanThreads, 0, st>>>(
+        d_jobs, d_items, count, plan, d_err);
+    using PieceSm = RowSmem<kPieceW, kPieceItems, false>;
+    const int smem = static_cast<int>(sizeof(PieceSm));
+    auto kern = num_piece_kernel<kPieceW, kPieceItems, kPieceMinB>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    kern<<<num_sms * kPieceMinB, kPieceW * 32, smem, st>>>(d_jobs, plan, d_stats, d_err, static_cast<double*>(slabs));
+    num_heavy_kernel<<<heavy_grid(count, num_sms), kHeavyThreads, 0, st>>>(
+        d_jobs, plan.fallback, count, slabs, max_ub, d_stats, d_err, plan.counters + 1);
+}
+
 void launch_numeric(int bin, const Job* d_jobs, const int64_t* d_items, int64_t count, int64_t max_ub,
-                    void* d_scratch, size_t scratch_bytes, Stats* d_stats, ErrWord* d_err, cudaStream_t st,
-                    int num_sms, bool holes, int variant) {
+                    const SplitTotals& split, void* d_scratch, size_t scratch_bytes, Stats* d_stats, ErrWord* d_err,
+                    cudaStream_t st, int num_sms, bool holes, int variant) {
     if (count <= 0) return;
     if (variant == 1 && launch_numeric_alt(bin, d_jobs, d_items, count, d_stats, d_err, st, num_sms)) return;
     if (bin <= kLastWarpBin) {
         launch_numeric_warp(bin, d_jobs, d_items, count, d_stats, d_err, st, num_sms);
+        return;
+    }
+    if (holes && bin > kLastSmemBin) {
+        launch_split(d_jobs, d_items, count, max_ub, split, d_scratch, d_stats, d_err, st, num_sms);
         return;
     }
     double* slab = static_cast<double*>(d_scratch);
@@ -467,7 +545,10 @@ void launch_numeric(int bin, const Job* d_jobs, const int64_t* d_items, int64_t 
             run_block<kB10W, kB10I, kB10MinB, kB10SV>(d_jobs, d_items, count, d_stats, d_err, st, num_sms,
                                                      tail_slab(d_scratch, scratch_bytes, cta_slab_bytes(10, count, num_sms)));
             break;
-        case 11: run_block<8, 6, 4>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;    // <= 1536
+        case 11:  // <= 1536
+            run_block<kB11W, kB11I, kB11MinB, kB11SV>(d_jobs, d_items, count, d_stats, d_err, st, num_sms,
+                                                     tail_slab(d_scratch, scratch_bytes, cta_slab_bytes(11, count, num_sms)));
+            break;
         case 12: run_block<8, 8, 4>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;    // <= 2048
         case 13:  // <= 3072
             run_block<kB13W, kB13I, kB13MinB, kB13SV>(d_jobs, d_items, count, d_stats, d_err, st, num_sms,
@@ -487,32 +568,9 @@ void launch_numeric(int bin, const Job* d_jobs, const int64_t* d_items, int64_t 
             break;
         case 17: run_block<16, 24, 1, false>(d_jobs, d_items, count, d_stats, d_err, st, num_sms, slab); break;
         case 18: run_block<16, 32, 1, false>(d_jobs, d_items, count, d_stats, d_err, st, num_sms, slab); break;
-        case kBinHeavy:
-            if (holes) {
-                const size_t global_slab = static_cast<size_t>(heavy_grid(count, num_sms)) * 24 * static_cast<size_t>(max_ub);
-                const size_t piece_slab = static_cast<size_t>(num_sms) * kPieceW * 32 * kPieceItems * sizeof(double);
-                const HeavyLayout L = heavy_layout(count, max_ub, std::max(global_slab, piece_slab));
-                unsigned char* base = static_cast<unsigned char*>(d_scratch);
-                HeavyPlan plan;
-                plan.counters = reinterpret_cast<unsigned long long*>(base);
-                plan.pieces = reinterpret_cast<Piece*>(base + L.pieces_off);
-                plan.fallback = reinterpret_cast<int64_t*>(base + L.fallback_off);
-                plan.max_pieces = L.max_pieces;
-                void* slabs = base + L.slab_off;
-                cudaMemsetAsync(plan.counters, 0, 2 * sizeof(unsigned long long), st);
-                heavy_plan_kernel<<<static_cast<int>(std::min<int64_t>(count, 2 * num_sms)), kPlanThreads, 0, st>>>(
-                    d_jobs, d_items, count, plan, d_err);
-                using PieceSm = RowSmem<kPieceW, kPieceItems, false>;
-                const int smem = static_cast<int>(sizeof(PieceSm));
-                cudaFuncSetAttribute(num_piece_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-                num_piece_kernel<<<num_sms, kPieceW * 32, smem, st>>>(d_jobs, plan, d_stats, d_err,
-                                                                      static_cast<double*>(slabs));
-                num_heavy_kernel<<<heavy_grid(count, num_sms), kHeavyThreads, 0, st>>>(
-                    d_jobs, plan.fallback, count, slabs, max_ub, d_stats, d_err, plan.counters + 1);
-            } else {
-                num_heavy_kernel<<<heavy_grid(count, num_sms), kHeavyThreads, 0, st>>>(
-                    d_jobs, d_items, count, d_scratch, max_ub, d_stats, d_err, nullptr);
-            }
+        case kBinHeavy:  // exact layout (the upper-bound layout splits these rows)
+            num_heavy_kernel<<<heavy_grid(count, num_sms), kHeavyThreads, 0, st>>>(
+                d_jobs, d_items, count, d_scratch, max_ub, d_stats, d_err, nullptr);
             break;
         default: break;
     }

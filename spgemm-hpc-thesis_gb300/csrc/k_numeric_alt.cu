@@ -14,7 +14,7 @@ bool launch_numeric_alt(int bin, const Job* d_jobs, const int64_t* d_items, int6
         case 8: run_block<2, 8, 8>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); return true;    // 512
         case 9: run_block<3, 8, 8>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); return true;    // 768
         case 10: run_block<4, 8, 6>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); return true;   // 1024
-        case 11: run_block<6, 8, 4>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); return true;   // 1536
+        case 11: run_block<8, 6, 4>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); return true;   // 1536
         case 12: run_block<4, 16, 4>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); return true;  // 2048
         case 13: run_block<8, 12, 2>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); return true;  // 3072
         case 14: run_block<16, 8, 1>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); return true;  // 4096

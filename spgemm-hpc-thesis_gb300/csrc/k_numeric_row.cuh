@@ -385,12 +385,15 @@ __device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double*
 
 
 // A column range of a split row: the products with columns in [lo, hi), which
-// own slots [slot_off, slot_off + count) of the row's reserved range.
+// own slots [slot_off, slot_off + count) of the row's reserved range.  The
+// row's products are staged in product order at scol / sval.
 struct Piece {
     int64_t item;
     int32_t lo, hi;
     int64_t slot_off;
     int64_t count;
+    const int32_t* scol;
+    const double* sval;
 };
 
 // One row (PIECE = false) or one column range of a row (PIECE = true, CTA
@@ -409,7 +412,7 @@ __device__ void numeric_row(const Job& J, int row, RowSmem<W, ITEMS, SV>& sm, do
     // 1. products into shared memory
     int32_t lo = INT32_MAX, hi = INT32_MIN;
     const int32_t ncols = J.B.cols;
-    auto take = [&](int32_t seq, int32_t c, double b, double a) {
+    auto put = [&](int32_t seq, int32_t c, double prod) {
         if (PIECE && seq >= P) {  // the planner counted fewer products in this range: never writes past P
             raise_error(err, kErrInvalid, 8, seq);
             return;
@@ -419,14 +422,18 @@ __device__ void numeric_row(const Job& J, int row, RowSmem<W, ITEMS, SV>& sm, do
             c = 0;
         }
         sm.keys[seq] = static_cast<uint32_t>(c);
-        vals[seq] = __dmul_rn(a, b);
+        vals[seq] = prod;
         lo = min(lo, c);
         hi = max(hi, c);
     };
     if constexpr (PIECE)
-        team_products_in<W * 32>(J, row, sm.seg, sm.warp_tmp, sm.step_cnt, tid, pc->lo, pc->hi, take);
+        staged_products_in<W * 32>(pc->scol, pc->sval, static_cast<int32_t>(J.ub[row]), sm.step_cnt, tid, pc->lo,
+                                   pc->hi, put);
     else
-        team_products<W * 32, true, int32_t>(J, row, sm.seg, sm.warp_tmp, tid, take);
+        team_products<W * 32, true, int32_t>(J, row, sm.seg, sm.warp_tmp, tid,
+                                             [&](int32_t seq, int32_t c, double b, double a) {
+                                                 put(seq, c, __dmul_rn(a, b));
+                                             });
     lo = warp_min(lo);
     hi = warp_max(hi);
     if (W > 1) {

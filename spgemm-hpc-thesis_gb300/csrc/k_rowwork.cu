@@ -28,12 +28,13 @@ __global__ void __launch_bounds__(kRowworkThreads)
 rowwork_kernel(const Job* __restrict__ jobs, int njobs, const int64_t* __restrict__ job_row_base,
                int64_t total_rows, Stats* __restrict__ stats, ErrWord* __restrict__ err) {
     __shared__ unsigned long long s_bins[kNumBins];
-    __shared__ unsigned long long s_products, s_max;
+    __shared__ unsigned long long s_products, s_max, s_split;
     const int lane = threadIdx.x & 31;
     if (threadIdx.x < kNumBins) s_bins[threadIdx.x] = 0;
     if (threadIdx.x == 0) {
         s_products = 0;
         s_max = 0;
+        s_split = 0;
     }
     __syncthreads();
 
@@ -70,6 +71,7 @@ rowwork_kernel(const Job* __restrict__ jobs, int njobs, const int64_t* __restric
             atomicAdd(&s_bins[bin_of(len)], 1ull);
             atomicAdd(&s_products, static_cast<unsigned long long>(len));
             atomicMax(&s_max, static_cast<unsigned long long>(len));
+            if (len > kSplitThreshold) atomicAdd(&s_split, static_cast<unsigned long long>(len));
         }
     }
     __syncthreads();
@@ -77,6 +79,7 @@ rowwork_kernel(const Job* __restrict__ jobs, int njobs, const int64_t* __restric
     if (threadIdx.x == 0) {
         atomicAdd(&stats->products, s_products);
         atomicMax(&stats->max_ub, s_max);
+        if (s_split) atomicAdd(&stats->split_products, s_split);
     }
 }
 

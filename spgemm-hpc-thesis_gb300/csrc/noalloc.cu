@@ -165,7 +165,7 @@ extern "C" spg_status spg_multiply_noalloc(const spg_csr_view* A, const spg_csr_
     int64_t bin_count[kNumBins];
     for (int b = 0; b < kNumBins; ++b) bin_count[b] = static_cast<int64_t>(hc.stats.bin_count[b]);
     const size_t slab = std::max(symbolic_scratch_bytes(bin_count, max_ub, num_sms),
-                                 numeric_scratch_bytes(bin_count, max_ub, num_sms, false, false));
+                                 numeric_scratch_bytes(bin_count, max_ub, SplitTotals{}, num_sms, false, false));
     unsigned char* d_slab = slab ? cv.take<unsigned char>(slab) : nullptr;
     if (!cv.fits())
         return ret(SPG_BUDGET_EXCEEDED, "heavy rows need more than the 32 MiB allocation-free scratch", err, err_len);
@@ -187,7 +187,7 @@ extern "C" spg_status spg_multiply_noalloc(const spg_csr_view* A, const spg_csr_
     if ((ce = cudaMemcpyAsync(d_job, &job, sizeof job, cudaMemcpyHostToDevice, st)) != cudaSuccess)
         return from_cuda(ce, "job update", err, err_len);
     for (int b = 1; b < kNumBins; ++b)
-        launch_numeric(b, d_job, items + hc.bin_off[b], static_cast<int64_t>(hc.stats.bin_count[b]), max_ub, d_slab,
+        launch_numeric(b, d_job, items + hc.bin_off[b], static_cast<int64_t>(hc.stats.bin_count[b]), max_ub, SplitTotals{}, d_slab,
                        slab, &d_ctrl->stats, &d_ctrl->err, st, num_sms, false);
     if ((ce = cudaMemcpyAsync(&hc, d_ctrl, sizeof hc, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
         (ce = cudaStreamSynchronize(st)) != cudaSuccess)

@@ -50,12 +50,15 @@ struct Job {
 //              <= 768, 1024, 1536, 2048, 3072, 4096, 6144, 8192
 //   bins 17-18 CTA per row, product values in a global slab: <= 12288, 16384
 //   bin 19     heavier rows: CTA per row, sort in global memory
+// In the upper-bound layout the rows of bins 17-19 (more than kSplitThreshold
+// products) are split by column range into pieces instead (k_numeric.cu).
 constexpr int kBinEmpty = 0;
 constexpr int kLastWarpBin = 8;     // capacity 512
 constexpr int kLastSmemBin = 16;    // capacity 8192
 constexpr int kBinHeavy = 19;
 constexpr int kNumBins = 20;
 constexpr int64_t kHeavyThreshold = 16384;
+constexpr int64_t kSplitThreshold = 8192;
 
 __host__ __device__ inline int clz64(unsigned long long x) {
 #ifdef __CUDA_ARCH__
@@ -106,6 +109,14 @@ struct Stats {
     unsigned long long bin_count[kNumBins];
     unsigned long long sym_total;     // sum of cnt
     unsigned long long nz_total;      // sum of nz
+    unsigned long long split_products;  // sum of ub over rows of more than kSplitThreshold products
+};
+
+// The rows of more than kSplitThreshold products of a call: their scalar
+// products (Stats::split_products) and their number (bins 17-19).
+struct SplitTotals {
+    int64_t products = 0;
+    int64_t rows = 0;
 };
 
 __device__ inline void raise_error(ErrWord* e, int32_t code, int32_t where, int64_t detail) {
@@ -187,12 +198,13 @@ size_t symbolic_scratch_bytes(const int64_t* bin_count, int64_t max_ub, int num_
 void launch_scan(int64_t* d_data, int64_t n, int64_t* d_partials, cudaStream_t stream);
 size_t scan_partials_count(int64_t n);
 // K4: sorted, summed, zero-free rows into job.c_col/c_val and job.nz[row].
-// holes: upper-bound layout (rows above 16384 products are then split into
-// column-range pieces; in the exact layout they keep the global-slab sort).
-// variant: 0 the default team shape of the bin, 1 its alternative (where the
-// bin has one; see launch_numeric_alt).
+// holes: upper-bound layout (rows above kSplitThreshold products are then
+// split into column-range pieces; in the exact layout they keep their CTA
+// kernels and the global-slab sort).  split: the call's totals of those rows
+// (they size the staging of split rows).  variant: 0 the default team shape of
+// the bin, 1 its alternative (where the bin has one; see launch_numeric_alt).
 void launch_numeric(int bin, const Job* d_jobs, const int64_t* d_items, int64_t count, int64_t max_ub,
-                    void* d_scratch, size_t scratch_bytes, Stats* d_stats, ErrWord* d_err,
+                    const SplitTotals& split, void* d_scratch, size_t scratch_bytes, Stats* d_stats, ErrWord* d_err,
                     cudaStream_t stream, int num_sms, bool holes, int variant = 0);
 // The alternative shape of a bin; false if the bin has none.
 bool launch_numeric_alt(int bin, const Job* d_jobs, const int64_t* d_items, int64_t count, Stats* d_stats,
@@ -201,10 +213,16 @@ constexpr int kNumVariants = 2;
 // K4 for the warp-per-row bins (1..kLastWarpBin), compiled separately.
 void launch_numeric_warp(int bin, const Job* d_jobs, const int64_t* d_items, int64_t count, Stats* d_stats,
                          ErrWord* d_err, cudaStream_t stream, int num_sms);
-// Global scratch of the numeric phase (value slabs of the 16K bin, sort slabs
-// of heavy rows; the two launches run one after the other and share it).
-size_t numeric_scratch_bytes(const int64_t* bin_count, int64_t max_ub, int num_sms, bool holes,
-                             bool concurrent = true);
+// Global scratch of the numeric phase: value slabs of the CTA bins, and for
+// the rows above 8192 products the staging and pieces of split rows (upper-
+// bound layout) or the slabs of their CTA kernels and global-slab sort.
+size_t numeric_scratch_bytes(const int64_t* bin_count, int64_t max_ub, const SplitTotals& split, int num_sms,
+                             bool holes, bool concurrent = true);
+// Totals of the split rows from the row-work statistics.
+inline SplitTotals split_totals(const Stats& st) {
+    return SplitTotals{static_cast<int64_t>(st.split_products),
+                       static_cast<int64_t>(st.bin_count[17] + st.bin_count[18] + st.bin_count[kBinHeavy])};
+}
 // K5: move rows from C_tmp (offsets job.cnt) to C (offsets job.nz, scanned).
 void launch_compact(const Job* d_job, int rows, int32_t* out_col, double* out_val, cudaStream_t stream);
 // K5 for rows written with holes: keeps the slots whose column is >= 0.

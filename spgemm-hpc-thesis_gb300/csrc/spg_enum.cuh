@@ -156,84 +156,55 @@ __device__ inline void team_products(const Job& J, int row, SegTab<NT, Idx>& tab
     }
 }
 
-// team_products restricted to the products whose column lies in [lo, hi), for
-// a whole CTA (NT threads, NT/32 <= 16 warps).  Kept products are numbered
-// 0, 1, ... in their row order (the order of team_products), so a stable sort
-// of the kept ones by column keeps the reference order of every column.  Each
-// step of 4*NT products compacts its kept flags with one ballot per product
-// slot and a scan of the 4*(NT/32) warp counts (s_cnt, 64 words).  Columns
-// outside [0, ncols) are treated as column 0, as in the unfiltered numeric
-// path (which reports them).  f(local_seq, col, b, a) as in team_products.
+// The products of a staged row (columns scol[0..n), values sval[0..n), in the
+// row's product order) whose column lies in [lo, hi), for a whole CTA (NT
+// threads, NT/32 <= 16 warps).  Kept products are numbered 0, 1, ... in row
+// order, so a stable sort of the kept ones by column keeps the reference order
+// of every column.  Each step of 4*NT products (coalesced loads) compacts its
+// kept flags with one ballot per product slot and a scan of the 4*(NT/32)
+// warp counts (s_cnt, 64 words).  f(local_seq, col, product) is called once
+// per kept product.
 template <int NT, typename F>
-__device__ inline void team_products_in(const Job& J, int row, SegTab<NT, int32_t>& tab, int64_t* s_warp,
-                                        uint32_t* s_cnt, int tid, int32_t lo, int32_t hi, F&& f) {
+__device__ inline void staged_products_in(const int32_t* __restrict__ scol, const double* __restrict__ sval,
+                                          int32_t n, uint32_t* s_cnt, int tid, int32_t lo, int32_t hi, F&& f) {
     constexpr int NW = NT / 32;
     static_assert(4 * NW <= 64, "at most 16 warps");
     const int lane = tid & 31, warp = tid >> 5;
-    const int32_t ncols = J.B.cols;
-    const bool has_s = J.S.rp != nullptr;
-    const int64_t a0 = J.A.rp[row];
-    const int64_t nseg = (J.A.rp[row + 1] - a0) + (has_s ? 1 : 0);
-    pad_segtab(tab, tid);
     int32_t kept_base = 0;
-    for (int64_t e0 = 0; e0 < nseg; e0 += NT) {
-        const int64_t e = e0 + tid;
-        const int32_t* cp = nullptr;
-        const double* vp = nullptr;
-        double sc = 1.0;
-        int32_t len = 0;
-        if (e < nseg) row_segment(J, row, a0, has_s, e, cp, vp, sc, len);
-        const int32_t incl = block_incl_scan<NT>(len, s_warp);
-        tab.colp[tid] = cp;
-        tab.valp[tid] = vp;
-        tab.scale[tid] = sc;
-        tab.incl[tid] = incl;
-        __syncthreads();
-        const int32_t total = tab.incl[NT - 1];
-        for (int32_t t0 = 0; t0 < total; t0 += 4 * NT) {  // uniform trip count: every thread reaches the barriers
-            int j[4];
-            int32_t c[4];
-            bool keep[4];
+    for (int32_t t0 = 0; t0 < n; t0 += 4 * NT) {  // uniform trip count: every thread reaches the barriers
+        int32_t c[4];
+        bool keep[4];
+        unsigned m[4];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int32_t t = t0 + u * NT + tid;
-                j[u] = t < total ? seg_search<NT>(tab.incl, t) : 0;
-                const int32_t q = t < total ? t - (j[u] ? tab.incl[j[u] - 1] : 0) : 0;
-                c[u] = t < total ? __ldg(tab.colp[j[u]] + q) : 0;
-                if (c[u] < 0 || c[u] >= ncols) c[u] = 0;
-                keep[u] = t < total && c[u] >= lo && c[u] < hi;
-            }
-            double b[4];
-            unsigned m[4];
+        for (int u = 0; u < 4; ++u) {
+            const int32_t t = t0 + u * NT + tid;
+            c[u] = t < n ? __ldg(scol + t) : 0;
+            keep[u] = t < n && c[u] >= lo && c[u] < hi;
+        }
+        double v[4];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int32_t t = t0 + u * NT + tid;
-                const int32_t q = keep[u] ? t - (j[u] ? tab.incl[j[u] - 1] : 0) : 0;
-                b[u] = keep[u] ? __ldg(tab.valp[j[u]] + q) : 0.0;
-                m[u] = __ballot_sync(0xffffffffu, keep[u]);
-                if (lane == 0) s_cnt[u * NW + warp] = static_cast<uint32_t>(__popc(m[u]));
-            }
-            __syncthreads();
-            // exclusive scan of the 4*NW counts in (u, warp) order, two per lane
-            const uint32_t x0 = 2 * lane < 4 * NW ? s_cnt[2 * lane] : 0u;
-            const uint32_t x1 = 2 * lane + 1 < 4 * NW ? s_cnt[2 * lane + 1] : 0u;
-            const uint32_t pair_incl = warp_incl_scan(x0 + x1, lane);
-            const uint32_t step_total = __shfl_sync(0xffffffffu, pair_incl, 31);
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int idx = u * NW + warp;
-                const uint32_t pi = __shfl_sync(0xffffffffu, pair_incl, idx >> 1);
-                const uint32_t p0 = __shfl_sync(0xffffffffu, x0, idx >> 1);
-                const uint32_t p1 = __shfl_sync(0xffffffffu, x1, idx >> 1);
-                const uint32_t excl = (pi - p0 - p1) + ((idx & 1) ? p0 : 0u);
-                if (keep[u])
-                    f(kept_base + static_cast<int32_t>(excl + __popc(m[u] & lanemask_lt())), c[u], b[u],
-                      tab.scale[j[u]]);
-            }
-            kept_base += static_cast<int32_t>(step_total);
-            __syncthreads();  // s_cnt is rewritten by the next step
+        for (int u = 0; u < 4; ++u) {
+            v[u] = keep[u] ? __ldg(sval + t0 + u * NT + tid) : 0.0;
+            m[u] = __ballot_sync(0xffffffffu, keep[u]);
+            if (lane == 0) s_cnt[u * NW + warp] = static_cast<uint32_t>(__popc(m[u]));
         }
         __syncthreads();
+        // exclusive scan of the 4*NW counts in (u, warp) order, two per lane
+        const uint32_t x0 = 2 * lane < 4 * NW ? s_cnt[2 * lane] : 0u;
+        const uint32_t x1 = 2 * lane + 1 < 4 * NW ? s_cnt[2 * lane + 1] : 0u;
+        const uint32_t pair_incl = warp_incl_scan(x0 + x1, lane);
+        const uint32_t step_total = __shfl_sync(0xffffffffu, pair_incl, 31);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int idx = u * NW + warp;
+            const uint32_t pi = __shfl_sync(0xffffffffu, pair_incl, idx >> 1);
+            const uint32_t p0 = __shfl_sync(0xffffffffu, x0, idx >> 1);
+            const uint32_t p1 = __shfl_sync(0xffffffffu, x1, idx >> 1);
+            const uint32_t excl = (pi - p0 - p1) + ((idx & 1) ? p0 : 0u);
+            if (keep[u]) f(kept_base + static_cast<int32_t>(excl + __popc(m[u] & lanemask_lt())), c[u], v[u]);
+        }
+        kept_base += static_cast<int32_t>(step_total);
+        __syncthreads();  // s_cnt is rewritten by the next step
     }
 }
 
