@@ -158,44 +158,47 @@ __device__ inline void team_products(const Job& J, int row, SegTab<NT, Idx>& tab
 
 // The products of a staged row (columns scol[0..n), values sval[0..n), in the
 // row's product order) whose column lies in [lo, hi), for a whole CTA (NT
-// threads, NT/32 <= 16 warps).  Kept products are numbered 0, 1, ... in row
+// threads, 8 * NT/32 <= 64).  Kept products are numbered 0, 1, ... in row
 // order, so a stable sort of the kept ones by column keeps the reference order
-// of every column.  Each step of 4*NT products (coalesced loads) compacts its
-// kept flags with one ballot per product slot and a scan of the 4*(NT/32)
+// of every column.  Each step of 8*NT products (coalesced loads, eight columns
+// per thread in flight: the staging is mostly read from DRAM) compacts its
+// kept flags with one ballot per product slot and a scan of the 8*(NT/32)
 // warp counts (s_cnt, 64 words).  f(local_seq, col, product) is called once
 // per kept product.
 template <int NT, typename F>
 __device__ inline void staged_products_in(const int32_t* __restrict__ scol, const double* __restrict__ sval,
                                           int32_t n, uint32_t* s_cnt, int tid, int32_t lo, int32_t hi, F&& f) {
     constexpr int NW = NT / 32;
-    static_assert(4 * NW <= 64, "at most 16 warps");
+    constexpr int U = 8;
+    static_assert(U * NW <= 64, "at most 8 warps");
     const int lane = tid & 31, warp = tid >> 5;
     int32_t kept_base = 0;
-    for (int32_t t0 = 0; t0 < n; t0 += 4 * NT) {  // uniform trip count: every thread reaches the barriers
-        int32_t c[4];
-        bool keep[4];
-        unsigned m[4];
+    for (int32_t t0 = 0; t0 < n; t0 += U * NT) {  // uniform trip count: every thread reaches the barriers
+        int32_t c[U];
+        bool keep[U];
+        unsigned m[U];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < U; ++u) {
             const int32_t t = t0 + u * NT + tid;
             c[u] = t < n ? __ldg(scol + t) : 0;
-            keep[u] = t < n && c[u] >= lo && c[u] < hi;
         }
-        double v[4];
+        double v[U];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            v[u] = keep[u] ? __ldg(sval + t0 + u * NT + tid) : 0.0;
+        for (int u = 0; u < U; ++u) {
+            const int32_t t = t0 + u * NT + tid;
+            keep[u] = t < n && c[u] >= lo && c[u] < hi;
+            v[u] = keep[u] ? __ldg(sval + t) : 0.0;
             m[u] = __ballot_sync(0xffffffffu, keep[u]);
             if (lane == 0) s_cnt[u * NW + warp] = static_cast<uint32_t>(__popc(m[u]));
         }
         __syncthreads();
-        // exclusive scan of the 4*NW counts in (u, warp) order, two per lane
-        const uint32_t x0 = 2 * lane < 4 * NW ? s_cnt[2 * lane] : 0u;
-        const uint32_t x1 = 2 * lane + 1 < 4 * NW ? s_cnt[2 * lane + 1] : 0u;
+        // exclusive scan of the U*NW counts in (u, warp) order, two per lane
+        const uint32_t x0 = 2 * lane < U * NW ? s_cnt[2 * lane] : 0u;
+        const uint32_t x1 = 2 * lane + 1 < U * NW ? s_cnt[2 * lane + 1] : 0u;
         const uint32_t pair_incl = warp_incl_scan(x0 + x1, lane);
         const uint32_t step_total = __shfl_sync(0xffffffffu, pair_incl, 31);
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < U; ++u) {
             const int idx = u * NW + warp;
             const uint32_t pi = __shfl_sync(0xffffffffu, pair_incl, idx >> 1);
             const uint32_t p0 = __shfl_sync(0xffffffffu, x0, idx >> 1);
