@@ -1,5 +1,6 @@
-// K4 numeric phase: row bins that run one row per CTA, the heavy rows, and the
-// bin dispatch (warp bins are compiled in k_numeric_warp.cu).  The per-row
+// K4 numeric phase: row bins that run one row per CTA, the rows above 8192
+// products (split into column-range pieces, or sorted in a global slab), and
+// the bin dispatch (warp bins are compiled in k_numeric_warp.cu).  The per-row
 // pipeline is in k_numeric_row.cuh.
 #include <algorithm>
 

@@ -19,9 +19,12 @@
 //      row's output offset (job.cnt[row]) and the kept count into job.nz[row].
 // Every coordinate is therefore bit-identical to the serial reference.  Rows of
 // <= 512 products run one per warp (num_warp_kernel), rows of <= 8192 one per
-// CTA with everything in shared memory, rows of <= 16384 one per CTA with the
-// product values in a global slab (num_block_kernel); heavier rows run one per
-// CTA with the whole sort in a global slab (num_heavy_kernel, k_numeric.cu).
+// CTA with the keys in shared memory and the values in shared memory or a
+// per-CTA global slab (num_block_kernel).  Heavier rows are split by column
+// range into pieces that run on the same pipeline (num_piece_kernel) in the
+// upper-bound layout; in the exact layout rows of <= 16384 run one per CTA with
+// a value slab and heavier ones with the whole sort in a global slab
+// (num_heavy_kernel, k_numeric.cu).
 #pragma once
 
 #include <type_traits>
