@@ -220,7 +220,8 @@ spg_status map_err(const ErrWord& e, std::string& msg) {
 }
 
 // The exact (symbolic) mode when asked for, or in auto mode when reserving
-// 12 bytes per scalar product would not fit the budget or half the free memory.
+// 12 bytes per slot would not fit the budget or half the free memory (slots:
+// the scalar products, plus the staged ones of rows above 8192 products).
 bool use_exact_mode(spg_handle* h, int64_t products, size_t reserved) {
     if (h->cfg.mode == SPG_MODE_EXACT) return true;
     if (h->cfg.mode == SPG_MODE_UPPER_BOUND) return false;
@@ -332,10 +333,11 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
     for (int b = 0; b <= kNumBins; ++b) bin_off[b] = hc->bin_off[b];
 
     // Output layout: in the upper-bound mode every row is written at the prefix
-    // of its product count (ub) and compacted afterwards; in the exact mode a
+    // of its product count (ub) and compacted afterwards, and the products of
+    // rows above 8192 are also staged (12 more bytes each); in the exact mode a
     // symbolic phase counts the distinct columns of every row first.
-    const bool exact = use_exact_mode(h, products, ar.bytes());
     const SplitTotals split = split_totals(hc->stats);
+    const bool exact = use_exact_mode(h, products + split.products, ar.bytes());
     size_t scratch_bytes = numeric_scratch_bytes(bin_count, max_ub, split, h->num_sms, !exact);
     if (exact) scratch_bytes = std::max(scratch_bytes, symbolic_scratch_bytes(bin_count, max_ub, h->num_sms));
     void* scratch = scratch_bytes ? ar.alloc<unsigned char>(scratch_bytes, "heavy scratch") : nullptr;
