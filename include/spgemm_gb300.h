@@ -353,11 +353,17 @@ spg_status spg_server_result_free(spg_server* server, spg_csr_result* C);
  * scratch would exceed it (roughly: 32 bytes per row of A plus 12 bytes per
  * distinct output coordinate) is rejected with SPG_BUDGET_EXCEEDED, as is an
  * nnz(C) above c_capacity (*c_nnz then holds the nnz needed).  The first call
- * on a device looks up the array's device address, so make it before any
- * stream capture.  Calls share the array: calls that overlap on the GPU race
- * and must be serialised by the caller.  Results are those of spg_multiply.
- * The call returns after the stream has finished the product; `err`
- * (err_len bytes, may be NULL) receives a message on failure. */
+ * on a device looks up the array's device address and is a warm-up: under
+ * CUDA's lazy module loading the first launch of each kernel loads its code,
+ * which may reserve device memory, so a caller that must see no change in
+ * device memory makes one call at start-up.  No call, first or later, may be
+ * made on a stream that is being captured: every call waits for its stream and
+ * reads control values back through pageable host memory (such a stream is
+ * rejected with SPG_INVALID_ARGUMENT).  The stream must belong to the current
+ * device.  Calls share the array: calls that overlap on the GPU race and must
+ * be serialised by the caller.  Results are those of spg_multiply.  The call
+ * returns after the stream has finished the product; `err` (err_len bytes, may
+ * be NULL) receives a message on failure. */
 spg_status spg_multiply_noalloc(const spg_csr_view* A, const spg_csr_view* B, void* stream, int64_t* c_row_ptr,
                                 int32_t* c_col, double* c_val, int64_t c_capacity, int64_t* c_nnz, char* err,
                                 size_t err_len);

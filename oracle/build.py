@@ -5,8 +5,8 @@
 * ``build_ref()`` compiles the reference's own local-multiply sources, in place
   from the read-only reference tree, together with ``ref_shim.cpp`` and the
   single-rank ``ref_stub/mpi.h``, into ``oracle/_ref/libspgemm_ref.so``.  It
-  needs the reference checkout (``REFERENCE_ROOT``, default /root/reference)
-  and is skipped where that tree is absent.
+  needs the reference checkout: ``REFERENCE_ROOT``, else a ``reference``
+  directory beside the repository; it is skipped where that tree is absent.
 
 Both libraries use -O3 -fopenmp -ffp-contract=off: the reference source
 multiplies and adds in separate statements, and the checkers keep those two
@@ -54,7 +54,8 @@ def build_oracle(force: bool = False) -> Path:
 
 
 def reference_root() -> Path:
-    return Path(os.environ.get("REFERENCE_ROOT", "/root/reference"))
+    env = os.environ.get("REFERENCE_ROOT")
+    return Path(env) if env else HERE.parents[1] / "reference"
 
 
 def build_ref(force: bool = False) -> Path | None:

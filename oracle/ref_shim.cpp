@@ -1,6 +1,6 @@
 // C entry points over the reference's own local-multiply sources, compiled in
 // place from the read-only reference tree into oracle/_ref/libspgemm_ref.so by
-// oracle/build_ref.py.  TEST INFRASTRUCTURE ONLY: it pins the oracle
+// build_ref() in oracle/build.py.  TEST INFRASTRUCTURE ONLY: it pins the oracle
 // restatement (oracle/spgemm_oracle.cpp) and generates the golden vectors.
 //
 // The reference's cached-oracle files (partial_reference.cpp,

@@ -5,7 +5,7 @@
 // C++17 + OpenMP, the reference algorithms of malchioman/SpGEMM-hpc-thesis for
 // the local multiply and its two validation oracles.  Every function cites the
 // reference file:line it follows.  Parity of this restatement is pinned against
-// the reference's own sources (oracle/_ref, built by oracle/build_ref.py) and
+// the reference's own sources (oracle/_ref, built by build_ref() in oracle/build.py) and
 // against the golden vectors under tests/golden/.
 //
 // Numerics: compiled with -ffp-contract=off so that `product = a*b; acc += product`

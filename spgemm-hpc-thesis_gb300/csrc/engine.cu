@@ -786,53 +786,65 @@ spg_status spg_multiply_to_host(spg_handle* h, const spg_csr_view* A, const spg_
             }
             held.clear();
         };
+        // On any failure after the first block (a capacity shortfall, an input
+        // error found in a later block, a CUDA error), copies of earlier blocks
+        // into the caller's host arrays may still be queued on the copy stream:
+        // wait for them before returning, so that the caller can free or reuse
+        // its buffers, and release the blocks and events.
+        auto abandon = [&] {
+            cudaStreamSynchronize(cs);
+            release_held();
+            for (auto e : done) cudaEventDestroy(e);
+            done.clear();
+        };
         c_row_ptr[0] = 0;
-        for (int k = 0; k < nchunks; ++k) {
-            const int32_t r0 = cut[k], r1 = cut[k + 1];
-            spg_csr_view blk = dv[0];
-            blk.rows = r1 - r0;
-            blk.row_ptr = dv[0].row_ptr + r0;  // absolute offsets into A's column/value arrays
-            std::vector<JobIn> in{{&blk, &dv[1], CsrView{}}};
-            std::vector<DevResult> out;
-            run_products(h, in, out, false, nullptr);
-            DevResult& r = out[0];
-            if (off + r.nnz > c_capacity) {
-                held.push_back(r);
-                cudaStreamSynchronize(cs);
-                release_held();
-                for (auto e : done) cudaEventDestroy(e);
-                *c_nnz = off + r.nnz;  // at least this many entries are needed
-                throw Failure{SPG_BUDGET_EXCEEDED, "nnz(C) exceeds c_capacity"};
+        try {
+            for (int k = 0; k < nchunks; ++k) {
+                const int32_t r0 = cut[k], r1 = cut[k + 1];
+                spg_csr_view blk = dv[0];
+                blk.rows = r1 - r0;
+                blk.row_ptr = dv[0].row_ptr + r0;  // absolute offsets into A's column/value arrays
+                std::vector<JobIn> in{{&blk, &dv[1], CsrView{}}};
+                std::vector<DevResult> out;
+                run_products(h, in, out, false, nullptr);
+                DevResult& r = out[0];
+                held.push_back(r);  // freed by release_held, on success or failure
+                if (off + r.nnz > c_capacity) {
+                    *c_nnz = off + r.nnz;  // at least this many entries are needed
+                    throw Failure{SPG_BUDGET_EXCEEDED, "nnz(C) exceeds c_capacity"};
+                }
+                // this block's offsets continue the previous ones; copy it out on the copy stream
+                launch_add_offset(r.rp + 1, r.rows, off, st);
+                cudaEvent_t e;
+                check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+                done.push_back(e);
+                check_cuda(cudaEventRecord(e, st), "event record");
+                check_cuda(cudaStreamWaitEvent(cs, e, 0), "stream wait");
+                check_cuda(cudaMemcpyAsync(c_row_ptr + r0 + 1, r.rp + 1, sizeof(int64_t) * r.rows, cudaMemcpyDeviceToHost, cs),
+                           "D2H row_ptr");
+                if (r.nnz) {
+                    check_cuda(cudaMemcpyAsync(c_col + off, r.ci, sizeof(int32_t) * r.nnz, cudaMemcpyDeviceToHost, cs),
+                               "D2H col");
+                    check_cuda(cudaMemcpyAsync(c_val + off, r.v, sizeof(double) * r.nnz, cudaMemcpyDeviceToHost, cs),
+                               "D2H val");
+                }
+                off += r.nnz;
+                sum.ms_rowwork += h->last.ms_rowwork;
+                sum.ms_symbolic += h->last.ms_symbolic;
+                sum.ms_scan += h->last.ms_scan;
+                sum.ms_numeric += h->last.ms_numeric;
+                sum.ms_compact += h->last.ms_compact;
+                sum.ms_total += h->last.ms_total;
+                sum.launches += h->last.launches + 1;
+                products += r.products;
+                for (int b = 0; b < kNumBins; ++b) {
+                    sum.bin_rows[b] += h->last.bin_rows[b];
+                    sum.ms_numeric_bin[b] += h->last.ms_numeric_bin[b];
+                }
             }
-            // this block's offsets continue the previous ones; copy it out on the copy stream
-            launch_add_offset(r.rp + 1, r.rows, off, st);
-            cudaEvent_t e;
-            check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
-            check_cuda(cudaEventRecord(e, st), "event record");
-            check_cuda(cudaStreamWaitEvent(cs, e, 0), "stream wait");
-            check_cuda(cudaMemcpyAsync(c_row_ptr + r0 + 1, r.rp + 1, sizeof(int64_t) * r.rows, cudaMemcpyDeviceToHost, cs),
-                       "D2H row_ptr");
-            if (r.nnz) {
-                check_cuda(cudaMemcpyAsync(c_col + off, r.ci, sizeof(int32_t) * r.nnz, cudaMemcpyDeviceToHost, cs),
-                           "D2H col");
-                check_cuda(cudaMemcpyAsync(c_val + off, r.v, sizeof(double) * r.nnz, cudaMemcpyDeviceToHost, cs),
-                           "D2H val");
-            }
-            held.push_back(r);
-            done.push_back(e);
-            off += r.nnz;
-            sum.ms_rowwork += h->last.ms_rowwork;
-            sum.ms_symbolic += h->last.ms_symbolic;
-            sum.ms_scan += h->last.ms_scan;
-            sum.ms_numeric += h->last.ms_numeric;
-            sum.ms_compact += h->last.ms_compact;
-            sum.ms_total += h->last.ms_total;
-            sum.launches += h->last.launches + 1;
-            products += r.products;
-            for (int b = 0; b < kNumBins; ++b) {
-                sum.bin_rows[b] += h->last.bin_rows[b];
-                sum.ms_numeric_bin[b] += h->last.ms_numeric_bin[b];
-            }
+        } catch (...) {
+            abandon();
+            throw;
         }
         check_cuda(cudaStreamSynchronize(cs), "copy stream");
         release_held();

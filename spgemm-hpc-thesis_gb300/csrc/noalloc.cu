@@ -13,10 +13,16 @@
 //
 // The array's host-side name is not a device address; its device address is
 // looked up once per device, with that device current, by the first call made
-// on that device (cudaGetSymbolAddress), so that first call should happen
-// before any stream capture.  Every call on a device shares the array and
-// finds the previous call's contents in it: the parts that must start at zero
-// are cleared on the caller's stream, and calls that overlap on the GPU (other
+// on that device (cudaGetSymbolAddress).  That first call is also a warm-up:
+// under CUDA's lazy module loading the first launch of each kernel loads its
+// code, and the driver may reserve device memory for it, so callers that must
+// see no change in device memory make one call at start-up.  Later calls with
+// the same kinds of rows launch the same kernels and reserve nothing.  No call
+// can be made on a stream that is being captured: every call waits for its
+// stream and copies through pageable host memory.  The stream must belong to
+// the current device.  Every call on a device shares the array and finds the
+// previous call's contents in it: the parts that must start at zero are
+// cleared on the caller's stream, and calls that overlap on the GPU (other
 // streams, other host threads) race on the array and must be serialised by
 // the caller.
 #include <cuda_runtime.h>
@@ -117,6 +123,16 @@ extern "C" spg_status spg_multiply_noalloc(const spg_csr_view* A, const spg_csr_
     int device = 0;
     cudaError_t ce = cudaGetDevice(&device);
     if (ce != cudaSuccess) return from_cuda(ce, "cudaGetDevice", err, err_len);
+    int stream_device = device;
+    if (st && (ce = cudaStreamGetDevice(st, &stream_device)) != cudaSuccess)
+        return from_cuda(ce, "cudaStreamGetDevice", err, err_len);
+    if (stream_device != device)
+        return ret(SPG_INVALID_ARGUMENT, "the stream belongs to another device than the current one", err, err_len);
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    if ((ce = cudaStreamIsCapturing(st, &capture)) != cudaSuccess)
+        return from_cuda(ce, "cudaStreamIsCapturing", err, err_len);
+    if (capture != cudaStreamCaptureStatusNone)
+        return ret(SPG_INVALID_ARGUMENT, "the stream is being captured; this entry point waits for it", err, err_len);
     int num_sms = 0;
     cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device);
     std::string msg;
@@ -155,6 +171,7 @@ extern "C" spg_status spg_multiply_noalloc(const spg_csr_view* A, const spg_csr_
     launch_rowwork(d_job, 1, d_row_base, m, &d_ctrl->stats, &d_ctrl->err, st);
     launch_bin_offsets(&d_ctrl->stats, d_ctrl->bin_off, st);
     launch_bin_scatter(d_job, 1, d_row_base, m, d_ctrl->bin_off, d_ctrl->cursor, items, st);
+    if ((ce = cudaGetLastError()) != cudaSuccess) return from_cuda(ce, "row work launch", err, err_len);
     if ((ce = cudaMemcpyAsync(&hc, d_ctrl, sizeof hc, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
         (ce = cudaStreamSynchronize(st)) != cudaSuccess)
         return from_cuda(ce, "row work", err, err_len);
@@ -174,6 +191,7 @@ extern "C" spg_status spg_multiply_noalloc(const spg_csr_view* A, const spg_csr_
         launch_symbolic(b, d_job, items + hc.bin_off[b], static_cast<int64_t>(hc.stats.bin_count[b]), max_ub, d_slab,
                         slab, &d_ctrl->stats, &d_ctrl->err, st, num_sms);
     launch_scan(cnt, static_cast<int64_t>(slots) - 1, partials, st);
+    if ((ce = cudaGetLastError()) != cudaSuccess) return from_cuda(ce, "symbolic launch", err, err_len);
     int64_t total = 0;
     if ((ce = cudaMemcpyAsync(&total, cnt + m, sizeof total, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
         (ce = cudaMemcpyAsync(&hc.err, &d_ctrl->err, sizeof hc.err, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
@@ -189,6 +207,7 @@ extern "C" spg_status spg_multiply_noalloc(const spg_csr_view* A, const spg_csr_
     for (int b = 1; b < kNumBins; ++b)
         launch_numeric(b, d_job, items + hc.bin_off[b], static_cast<int64_t>(hc.stats.bin_count[b]), max_ub, SplitTotals{}, d_slab,
                        slab, &d_ctrl->stats, &d_ctrl->err, st, num_sms, false);
+    if ((ce = cudaGetLastError()) != cudaSuccess) return from_cuda(ce, "numeric launch", err, err_len);
     if ((ce = cudaMemcpyAsync(&hc, d_ctrl, sizeof hc, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
         (ce = cudaStreamSynchronize(st)) != cudaSuccess)
         return from_cuda(ce, "numeric phase", err, err_len);

@@ -1,7 +1,7 @@
 """Generates tests/golden/golden.npz from the reference's own code.
 
-Run in a checkout where the reference tree is available (REFERENCE_ROOT,
-default /root/reference): it builds oracle/_ref (the reference's sources,
+Run in a checkout where the reference tree is available (REFERENCE_ROOT, else
+a ``reference`` directory beside the repository): it builds oracle/_ref (the reference's sources,
 compiled unchanged with a single-rank MPI stand-in), reads the reference's
 Matrix Market fixtures with the reference's reader, and records for every case
 the inputs and the outputs of the reference's serialSpgemm, spgemm() (the

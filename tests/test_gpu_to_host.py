@@ -72,3 +72,33 @@ def test_empty_and_errors(engine):
     with pytest.raises(SpgError) as e:
         to_host(engine, bad, Csr.from_arrays(3, 2, [0, 1, 2, 3], [0, 1, 0], [1.0, 1.0, 1.0]), cap=10)
     assert e.value.name == "SPG_OUT_OF_RANGE_COLUMN"
+
+
+@pytest.mark.parametrize("pinned", [False, True])
+def test_error_in_a_late_block_waits_for_earlier_copies(engine, pinned):
+    # 6.3 M entries in A, so the product runs in ten row blocks; one A column in
+    # the last rows points past B's rows, so the call fails in the last block,
+    # after the copies of the earlier blocks into the host arrays have started.
+    # The call must return only once those copies are done: the arrays do not
+    # change after it returns, and the handle stays usable.
+    import time
+    import torch
+    a = synth_powerlaw(262144, 24.0, 1.2, 20000, 2048, 0.7, seed=3)
+    bad = Csr(a.rows, a.cols, a.row_ptr.copy(), a.col.copy(), a.val.copy())
+    bad.col[int(bad.row_ptr[-2])] = a.cols  # last row: column == B.rows
+    cap = engine.scalar_multiplication_count(a, a)
+    if pinned:
+        bufs = [torch.full((n,), -7, dtype=t, pin_memory=True)
+                for n, t in ((a.rows + 1, torch.int64), (cap, torch.int32), (cap, torch.float64))]
+    else:
+        bufs = [np.full(a.rows + 1, -7, np.int64), np.full(cap, -7, np.int32), np.full(cap, -7.0, np.float64)]
+    with pytest.raises(SpgError) as e:
+        engine.multiply_to_host(bad, a, *bufs)
+    assert e.value.name == "SPG_OUT_OF_RANGE_COLUMN"
+    snap = [np.asarray(x).copy() for x in bufs]
+    assert (snap[1] != -7).any(), "earlier blocks were copied out before the failing one"
+    time.sleep(0.2)
+    assert all(np.array_equal(np.asarray(x), s) for x, s in zip(bufs, snap))
+    got = to_host(engine, a, a, pinned=pinned)
+    want = engine.multiply(a.to_device(), a.to_device(), out="device").download()
+    assert csr_bits_equal(got, want), explain_diff(got, want)

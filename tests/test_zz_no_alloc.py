@@ -46,7 +46,7 @@ def same(x, y) -> bool:
             and np.array_equal(x.val.view(np.uint64), y.val.view(np.uint64)))
 
 
-def test_noalloc_matches_multiply_twice():
+def test_noalloc_matches_multiply_twice(port):
     lib = sg.library()
     lib.spg_multiply_noalloc.restype = C.c_int
     cases = [row_sizes_for_bins(3),
@@ -55,11 +55,45 @@ def test_noalloc_matches_multiply_twice():
     with sg.Engine(0) as eng:
         for a, b in cases:
             want = eng.multiply(a, b)
+            assert same(want, port.serial_spgemm(a, b))  # both equal the serial reference product
             da, db = a.to_device(), b.to_device()
             for _ in range(2):  # the second call reuses the scratch left by the first
                 st, n, msg, got = noalloc(lib, da, db, want.nnz)
                 assert st == 0, msg
                 assert n == want.nnz and same(got, want)
+
+
+def test_noalloc_second_call_reserves_no_device_memory():
+    # The first call on a device is the warm-up (it may load kernel code); a
+    # second call on the same operands, into the same output arrays, must leave
+    # the device's free memory unchanged.
+    import torch
+    lib = sg.library()
+    lib.spg_multiply_noalloc.restype = C.c_int
+    a, b = row_sizes_for_bins(5)
+    da, db = a.to_device(), b.to_device()
+    with sg.Engine(0) as eng:
+        cap = eng.multiply(a, b).nnz
+    rp = torch.zeros(da.rows + 1, dtype=torch.int64, device="cuda")
+    ci = torch.zeros(cap, dtype=torch.int32, device="cuda")
+    va = torch.zeros(cap, dtype=torch.float64, device="cuda")
+    nnz = C.c_int64(-1)
+    err = C.create_string_buffer(256)
+    va_view, vb_view = sg._dev_view(da), sg._dev_view(db)
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def call():
+        return lib.spg_multiply_noalloc(C.byref(va_view), C.byref(vb_view), C.c_void_p(stream),
+                                        C.c_void_p(rp.data_ptr()), C.c_void_p(ci.data_ptr()),
+                                        C.c_void_p(va.data_ptr()), C.c_int64(cap), C.byref(nnz), err,
+                                        C.c_size_t(256))
+    assert call() == 0, err.value
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    assert call() == 0, err.value
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free_before
+    assert nnz.value == cap
 
 
 def test_noalloc_rejects_beyond_limits():
