@@ -149,6 +149,18 @@ spg_status spg_result_free(spg_handle* handle, spg_csr_result* C);
 spg_status spg_scalar_multiplication_count(spg_handle* handle, const spg_csr_view* A, const spg_csr_view* B,
                                            int64_t* products);
 
+/* Row blocks for multi-GPU row sharding: first_row[0..parts] (parts + 1
+ * entries) cut A's rows into `parts` contiguous blocks of about equal scalar
+ * products -- first_row[k] is the first row whose preceding products reach
+ * floor(k * P / parts), first_row[0] = 0, first_row[parts] = A.rows -- so that
+ * G GPUs each multiplying one block against a replicated B get about P / G
+ * products each.  Replaces std::vector<RowBlock> partitionRows(int, int)
+ * (src/common/spgemm_common.cpp:326-337), which splits by row count; with no
+ * products at all the split is by row count as there.  Errors as
+ * spg_scalar_multiplication_count. */
+spg_status spg_partition_rows(spg_handle* handle, const spg_csr_view* A, const spg_csr_view* B, int32_t parts,
+                              int32_t* first_row);
+
 /* Per-phase timings of the last spg_multiply / spg_accum_add on the handle. */
 spg_status spg_last_timings(const spg_handle* handle, spg_timings* timings);
 

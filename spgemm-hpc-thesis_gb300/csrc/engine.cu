@@ -887,6 +887,54 @@ spg_status spg_scalar_multiplication_count(spg_handle* h, const spg_csr_view* A,
     });
 }
 
+spg_status spg_partition_rows(spg_handle* h, const spg_csr_view* A, const spg_csr_view* B, int32_t parts,
+                              int32_t* first_row) {
+    return guarded(h, [&] {
+        require(parts >= 1 && first_row != nullptr, SPG_INVALID_ARGUMENT, "parts must be >= 1, first_row non-NULL");
+        check_view(A, "A");
+        check_view(B, "B");
+        require(A->cols == B->rows, SPG_INVALID_ARGUMENT, "SpGEMM requires A.cols == B.rows");
+        cudaStream_t st = h->stream;
+        Arena ar(h);
+        Job job;
+        job.A = stage(h, ar, A);
+        const bool same = A->location == B->location && A->row_ptr == B->row_ptr && A->col == B->col &&
+                          A->val == B->val && A->rows == B->rows && A->cols == B->cols && A->nnz == B->nnz;
+        job.B = same ? job.A : stage(h, ar, B);
+        const int64_t m = A->rows;
+        int64_t* ub = ar.alloc<int64_t>(static_cast<size_t>(m) + 1, "row products");
+        int64_t* cnt = ar.alloc<int64_t>(static_cast<size_t>(m) + 1, "row reservation");
+        job.ub = ub;
+        job.cnt = cnt;
+        int64_t* d_row_base = ar.alloc<int64_t>(2, "row base");
+        Ctrl* d_ctrl = ar.alloc<Ctrl>(1, "ctrl");
+        Job* d_job = ar.alloc<Job>(1, "job");
+        const size_t first_words = (static_cast<size_t>(parts) + 2) / 2;  // parts + 1 int32, read in 8-byte words
+        int32_t* d_first = ar.alloc<int32_t>(2 * first_words, "first rows");
+        int64_t* partials = ar.alloc<int64_t>(scan_partials_count(m + 1), "scan partials");
+        const int64_t rb[2] = {0, m};
+        check_cuda(cudaMemsetAsync(ub, 0, sizeof(int64_t) * (static_cast<size_t>(m) + 1), st), "memset");
+        check_cuda(cudaMemsetAsync(d_ctrl, 0, sizeof(Ctrl), st), "memset ctrl");
+        check_cuda(cudaMemcpyAsync(d_row_base, rb, sizeof rb, cudaMemcpyHostToDevice, st), "H2D row base");
+        check_cuda(cudaMemcpyAsync(d_job, &job, sizeof job, cudaMemcpyHostToDevice, st), "H2D job");
+        launch_rowwork(d_job, 1, d_row_base, m, &d_ctrl->stats, &d_ctrl->err, st);
+        launch_scan(ub, m, partials, st);  // exclusive, ub[m] = all scalar products
+        launch_partition(ub, m, parts, d_first, st);
+        check_cuda(cudaGetLastError(), "partition launch");
+        Ctrl* hc = static_cast<Ctrl*>(h->ctrl);
+        void* hf = host_staging(h, 8 * first_words);
+        launch_readback(&d_ctrl->err, &hc->err, sizeof(ErrWord), st);
+        launch_readback(d_first, hf, 8 * first_words, st);
+        sync(h);  // rb and job must outlive their copies
+        if (hc->err.code) {
+            std::string msg;
+            const spg_status status = map_err(hc->err, msg);
+            throw Failure{status, msg};
+        }
+        std::memcpy(first_row, hf, sizeof(int32_t) * (static_cast<size_t>(parts) + 1));
+    });
+}
+
 spg_status spg_scalar_multiplication_count_batch(spg_handle* h, int32_t n, const spg_csr_view* A,
                                                  const spg_csr_view* B, int64_t* products) {
     return guarded(h, [&] {

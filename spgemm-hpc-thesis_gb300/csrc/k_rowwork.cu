@@ -398,6 +398,44 @@ void launch_job_products(const Job* d_jobs, int njobs, const int64_t* d_job_row_
     job_products_kernel<<<njobs, 256, 0, stream>>>(d_jobs, d_job_row_base, d_out);
 }
 
+namespace {
+
+// Split points of `rows` rows into `parts` contiguous blocks of about equal
+// scalar products: first[k] is the first row whose preceding products reach
+// floor(k * total / parts) (prefix: exclusive scan of the per-row products,
+// prefix[rows] = total); first[0] = 0, first[parts] = rows.  With no products
+// at all the rows are split by count, as the reference's partitionRows does.
+__global__ void partition_kernel(const int64_t* __restrict__ prefix, int64_t rows, int32_t parts,
+                                 int32_t* __restrict__ first) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k > parts) return;
+    const int64_t total = prefix[rows];
+    int64_t r;
+    if (k == 0) {
+        r = 0;
+    } else if (k == parts) {
+        r = rows;
+    } else if (total == 0) {
+        r = rows * k / parts;
+    } else {
+        const int64_t target = static_cast<int64_t>(static_cast<unsigned __int128>(total) * k / parts);
+        int64_t lo = 0, hi = rows;  // smallest i with prefix[i] >= target
+        while (lo < hi) {
+            const int64_t mid = (lo + hi) >> 1;
+            if (prefix[mid] >= target) hi = mid;
+            else lo = mid + 1;
+        }
+        r = lo;
+    }
+    first[k] = static_cast<int32_t>(r);
+}
+
+}  // namespace
+
+void launch_partition(const int64_t* d_prefix, int64_t rows, int32_t parts, int32_t* d_first, cudaStream_t stream) {
+    partition_kernel<<<(parts + 1 + 127) / 128, 128, 0, stream>>>(d_prefix, rows, parts, d_first);
+}
+
 void launch_readback(const void* d_src, void* h_dst, size_t bytes, cudaStream_t stream) {
     if (bytes == 0) return;
     readback_kernel<<<1, 256, 0, stream>>>(static_cast<const unsigned long long*>(d_src),

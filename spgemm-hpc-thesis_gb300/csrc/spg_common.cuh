@@ -260,6 +260,9 @@ void launch_readback(const void* d_src, void* h_dst, size_t bytes, cudaStream_t 
 // batch (product j's rows + 1 entries start at job_row_base[j] + j in both).
 void launch_rebase_jobs(const int64_t* d_scanned, int64_t* d_out, const int64_t* d_job_row_base, int njobs,
                         int64_t max_rows, cudaStream_t stream);
+// Row blocks of about equal scalar products (spg_partition_rows): d_first
+// (parts + 1 entries) from the exclusive scan of the per-row products.
+void launch_partition(const int64_t* d_prefix, int64_t rows, int32_t parts, int32_t* d_first, cudaStream_t stream);
 // d[i] += add for i < n.
 void launch_add_offset(int64_t* d, int64_t n, int64_t add, cudaStream_t stream);
 // Scalar products of every product of a batch (after K1): out[j] = sum of job j's ub.

@@ -173,7 +173,7 @@ def library() -> C.CDLL:
                      "spg_config_default", "spg_server_create", "spg_submit", "spg_poll", "spg_cancel",
                      "spg_server_result_free", "spg_plan_create", "spg_plan_execute", "spg_plan_result", "spg_tune",
                      "spg_get_bin_variants", "spg_set_bin_variants", "spg_validate_full", "spg_transpose",
-                     "spg_read_matrix_market"):
+                     "spg_read_matrix_market", "spg_partition_rows"):
             getattr(lib, name).restype = C.c_int
         _lib = lib
     return _lib
@@ -384,6 +384,15 @@ class Engine:
         self._check(library().spg_scalar_multiplication_count_batch(self.h, C.c_int32(n), A, B, P))
         return [int(P[i]) for i in range(n)]
 
+    def partition_rows(self, a, b, parts: int) -> np.ndarray:
+        """spg_partition_rows: first_row[0..parts] cutting A's rows into blocks of
+        about equal scalar products (device row work)."""
+        keep: list = []
+        va, vb = _view(a, keep), _view(b, keep)
+        out = (C.c_int32 * (parts + 1))()
+        self._check(library().spg_partition_rows(self.h, C.byref(va), C.byref(vb), C.c_int32(parts), out))
+        return np.frombuffer(out, dtype=np.int32).copy()
+
     def scalar_multiplication_count(self, a, b) -> int:
         keep: list = []
         va, vb = _view(a, keep), _view(b, keep)
@@ -455,6 +464,23 @@ class Plan:
             pass
 
 
+def _cudart() -> C.CDLL:
+    """The CUDA runtime the engine library is linked against (already loaded
+    with it): found by its soname, else by its path in this process's maps."""
+    library()
+    for name in ("libcudart.so", "libcudart.so.13", "libcudart.so.12"):
+        try:
+            return C.CDLL(name)
+        except OSError:
+            pass
+    with open("/proc/self/maps") as f:
+        for line in f:
+            path = line.split()[-1]
+            if "libcudart.so" in path:
+                return C.CDLL(path)
+    raise RuntimeError("the CUDA runtime library is not loaded")
+
+
 def read_matrix_market(path, out: str = "host"):
     """spg_read_matrix_market: the reference's readMatrixMarket semantics
     (matrix_market.cpp:28-145).  out="host" returns a Csr; out="device" a
@@ -481,7 +507,7 @@ def read_matrix_market(path, out: str = "host"):
         ci = torch.empty(max(res.nnz, 1), dtype=torch.int32, device=dev)
         va = torch.empty(max(res.nnz, 1), dtype=torch.float64, device=dev)
         torch.cuda.synchronize()
-        cudart = C.CDLL("libcudart.so")
+        cudart = _cudart()
         for dst, src, nb in ((rp, res.row_ptr, 8 * (res.rows + 1)), (ci, res.col, 4 * res.nnz), (va, res.val, 8 * res.nnz)):
             if nb and cudart.cudaMemcpy(C.c_void_p(dst.data_ptr()), C.c_void_p(src), C.c_size_t(nb), 3) != 0:
                 raise SpgError(7, "device copy failed")

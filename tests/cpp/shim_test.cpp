@@ -8,6 +8,11 @@
 
 #include "spgemm_gb300.hpp"
 
+#ifdef SPG_REFERENCE_CSR
+// The reference's own type (src/common/csr_matrix.hpp:43-49), where its tree is
+// on the include path.
+#include "csr_matrix.hpp"
+#else
 struct CsrMatrix {  // the layout of src/common/csr_matrix.hpp:43-49
     int rows = 0;
     int cols = 0;
@@ -15,6 +20,13 @@ struct CsrMatrix {  // the layout of src/common/csr_matrix.hpp:43-49
     std::vector<int> columnIndices;
     std::vector<double> values;
 };
+#endif
+
+// The substitution a Trident build makes for its accumulator
+// (src/trident/common/matrix_blocks.hpp:23-32).
+namespace trident {
+using LocalAccumulator = spgemm_gb300::LocalAccumulator<CsrMatrix>;
+}
 
 #define REQUIRE(x)                                                   \
     do {                                                             \
@@ -60,7 +72,7 @@ int main() {
     CsrMatrix sa{3, 2, {0, 3, 3, 4}, {1, 0, 1, 0}, {2.0, 1.0, -1.0, 3.0}};
     const CsrMatrix sb{2, 4, {0, 3, 5}, {3, 1, 3, 0, 1}, {2.0, 4.0, -1.0, 5.0, -4.0}};
     {
-        g::LocalAccumulator<CsrMatrix> acc(3, 4);
+        trident::LocalAccumulator acc(3, 4);
         acc.addProduct(sa, sb);
         for (auto& v : sa.values) v *= -1.0;
         acc.addProduct(sa, sb);
@@ -80,7 +92,7 @@ int main() {
         REQUIRE(caught);
     }
     {
-        g::LocalAccumulator<CsrMatrix> empty(0, 4);
+        trident::LocalAccumulator empty(0, 4);
         REQUIRE(empty.finish().rowPtr == std::vector<int64_t>{0});
     }
     // the reference's validation, its Matrix Market reader and a transposition, through the same layer
