@@ -19,9 +19,10 @@ reference's definition, two_sided_spgemm.cpp:188-192).
   a bounded slice of A's rows, timed on this host's cores.
 
 --impl reference runs only the CPU reference on the same workload and prints
-its own line.  With torchrun (N > 1) every rank runs an independent replica on
-its own GPU (the path's multi-GPU row sharding is not built); value sums the
-ranks' products over the slowest rank's time.
+its own line.  With torchrun (N > 1) the rows of every product are sharded:
+each rank multiplies the block of A's rows holding about P / N scalar products
+against all of B on its own GPU (no collective inside the timed region), and
+value sums the ranks' products over the slowest rank's time (strong scaling).
 """
 from __future__ import annotations
 
@@ -55,10 +56,11 @@ WORKLOADS = {
 }
 BATCH_PRODUCTS = 512
 BATCH_MAX_PRODUCTS = 1 << 28  # scalar products per batch: ~8 ms of kernels, so the two lanes alternate
+BATCH_SUBSET = 64  # products of the batched workload measured beside the headline line
 SERVE_RATES = (50, 100, 200, 500, 1000, 2000)
 
 
-def make_workload(name: str, rows: int = 0):
+def make_workload(name: str, rows: int = 0, count: int = 0):
     """[(A, B)] host operands of the workload's products (chained products are
     materialised once on the host).  rows != 0 shrinks the power-law matrix
     (profiling cases only)."""
@@ -78,6 +80,8 @@ def make_workload(name: str, rows: int = 0):
     if name == "batched":
         rng = np.random.default_rng(4)
         sizes = np.exp(rng.uniform(np.log(1000), np.log(200000), size=BATCH_PRODUCTS)).astype(np.int64)
+        if count:
+            sizes = sizes[:count]
         return [(sg.synth_uniform(int(n), int(n), 4, 64, seed=2 * i + 1),
                  sg.synth_uniform(int(n), int(n), 4, 64, seed=2 * i + 2)) for i, n in enumerate(sizes)]
     if name == "served":
@@ -283,36 +287,23 @@ def run_reference_arm(args, rank, world):
 
 
 # ---------------------------------------------------------------------------
-def run_gpu_arm(args, rank, world, local):
+def device_measure(eng, pairs, dev_pairs, steps: int, warmup: int, local: int, world: int = 1):
+    """Device-timed steps of one workload: every step multiplies all of its
+    products with device-resident operands (results left on the device and
+    freed), between CUDA events on the engine's stream; inputs smaller than L2
+    get a 512 MiB write between steps, outside the events.  Returns the
+    measurement, the roofline of the numeric phase and the bookkeeping."""
     import torch
     import spgemm_gb300 as sg
-    torch.cuda.set_device(local)
-    pairs = make_workload(args.workload, args.rows)
-    eng = sg.Engine(local)
-    dev_pairs = []
-    for a, b in pairs:
-        da = a.to_device(local)
-        db = da if b is a else b.to_device(local)
-        dev_pairs.append((da, db))
     products = sum(sg.scalar_products_host(a, b) for a, b in pairs)
-
-    # one untimed product per pair to learn nnz(C) (for the byte count and D2H size)
     c_nnz = []
-    for da, db in dev_pairs:
+    for da, db in dev_pairs:  # one untimed product per pair: nnz(C) for the byte count
         r = eng.multiply(da, db, out="device")
         c_nnz.append(r.nnz)
         r.free()
     bytes_alg = sum(sg.algorithmic_bytes(a, b, sg.scalar_products_host(a, b), n)
                     for (a, b), n in zip(pairs, c_nnz))
-
-    # bin autotuner (untimed setup): per-bin team shape chosen by measured time on this workload
-    tuned = None
-    if not args.no_tune:
-        da, db = dev_pairs[0]
-        tuned = eng.tune(da, db, reps=2)
-
     stream = torch.cuda.ExternalStream(eng.stream, device=torch.device("cuda", local))
-
     last_phases: dict = {}
 
     def step():
@@ -328,17 +319,14 @@ def run_gpu_arm(args, rank, world, local):
         last_phases.update({k: v for k, v in t.items() if k.startswith("ms_")})
         return launches, numeric_ms
 
-    # Inputs below the L2 size get a 512 MiB write between timed steps (outside
-    # the events), so that no step starts with its operands already in L2.
     in_bytes = sum(_csr_bytes(a) + (0 if b is a else _csr_bytes(b)) for a, b in pairs)
     flush = in_bytes < L2_BYTES
     flush_buf = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}") if flush else None
-
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step()
     barrier(world)
     torch.cuda.synchronize()
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     launches = 0
     numeric_ms = 0.0
     with ClockSampler(local) as clocks:
@@ -355,6 +343,107 @@ def run_gpu_arm(args, rank, world, local):
     torch.cuda.synchronize()
     barrier(world)
     t_ms = sum(e0.elapsed_time(e1) for e0, e1 in evs)
+    pk = peaks()
+    numeric_avg_s = numeric_ms / steps / 1e3
+    achieved = bytes_alg / numeric_avg_s / 1e9 if numeric_avg_s > 0 else None
+    roofline = {"bound": "hbm", "kernel": "K4 numeric phase (all bins, one step)", "achieved": achieved,
+                "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": (achieved / pk["hbm_gbs"]) if achieved else None,
+                "peak_source": pk["source"], "bytes_alg": int(bytes_alg),
+                "pipeline_frac": bytes_alg / (t_ms / steps / 1e3) / 1e9 / pk["hbm_gbs"]}
+    return {"t_ms": t_ms, "products": products, "c_nnz": c_nnz, "launches": launches, "roofline": roofline,
+            "phases": dict(last_phases), "clocks": clocks.summary(), "flush": flush, "in_bytes": in_bytes}
+
+
+def sub_record(name: str, steps: int, warmup: int, local: int) -> dict:
+    """A secondary workload measured in the same run as the headline one."""
+    import spgemm_gb300 as sg
+    pairs = make_workload(name)
+    with sg.Engine(local) as eng:
+        dev_pairs = []
+        for a, b in pairs:
+            da = a.to_device(local)
+            dev_pairs.append((da, da if b is a else b.to_device(local)))
+        m = device_measure(eng, pairs, dev_pairs, steps, warmup, local)
+    return {"workload": WORKLOADS[name], "value": 2.0 * m["products"] * steps / (m["t_ms"] / 1e3) / 1e9,
+            "unit": "GFLOP/s", "steps": steps, "warmup": warmup, "ms_per_step": m["t_ms"] / steps,
+            "products_per_step": int(m["products"]), "c_nnz": int(sum(m["c_nnz"])),
+            "l2": "L2 flushed between timed steps (512 MiB write outside the events)" if m["flush"]
+                  else "inputs larger than L2", "roofline": m["roofline"],
+            "phases_ms_last_step": {k: v for k, v in m["phases"].items() if k != "ms_numeric_bin"},
+            "gpu_launches": int(m["launches"])}
+
+
+def batched_subset_record(local: int, count: int = BATCH_SUBSET) -> dict:
+    """A seeded subset of the batched workload's products (the first `count` of
+    its 512, same size distribution) through one spg_multiply_batch call per
+    step, against the same products one spg_multiply call each."""
+    import spgemm_gb300 as sg
+    pairs = make_workload("batched", count=count)
+    products = sum(sg.scalar_products_host(a, b) for a, b in pairs)
+    with sg.Engine(local) as eng:
+        dev = [(a.to_device(local), b.to_device(local)) for a, b in pairs]
+
+        def batched():
+            for r in eng.multiply_batch(dev, out="device"):
+                r.free()
+            return eng.last_timings()["launches"]
+
+        def one_by_one():
+            launches = 0
+            for a, b in dev:
+                eng.multiply(a, b, out="device").free()
+                launches += eng.last_timings()["launches"]
+            return launches
+
+        for _ in range(2):
+            batched()
+            one_by_one()
+        reps = 3
+        tb = sum(_wall(batched)[0] for _ in range(reps)) / reps
+        ts = sum(_wall(one_by_one)[0] for _ in range(reps)) / reps
+        lb, ls = batched(), one_by_one()
+    return {"workload": WORKLOADS["batched"] + f" [first {count} of {BATCH_PRODUCTS} products]",
+            "products": count, "rows_total": int(sum(a.rows for a, _ in pairs)),
+            "scalar_products_per_step": int(products), "steps": reps,
+            "timing": "host wall clock between device synchronisations",
+            "batched": {"value": 2.0 * products / tb / 1e9, "unit": "GFLOP/s", "ms_per_step": 1e3 * tb,
+                        "gpu_launches_per_step": int(lb), "what": "one spg_multiply_batch call"},
+            "per_product": {"value": 2.0 * products / ts / 1e9, "unit": "GFLOP/s", "ms_per_step": 1e3 * ts,
+                            "gpu_launches_per_step": int(ls), "what": "one spg_multiply call per product"},
+            "batched_over_per_product": ts / tb}
+
+
+def run_gpu_arm(args, rank, world, local):
+    import torch
+    import spgemm_gb300 as sg
+    torch.cuda.set_device(local)
+    pairs = make_workload(args.workload, args.rows)
+    if world > 1:
+        # row sharding: this rank's block of A's rows (about P / world scalar
+        # products, cut by the prefix of the row products) against all of B
+        import sharding
+        sharded = []
+        for a, b in pairs:
+            first = sharding.partition_rows(a, b, world)
+            sharded.append((sharding.slice_rows(a, int(first[rank]), int(first[rank + 1] - first[rank])), b))
+        pairs = sharded
+    eng = sg.Engine(local)
+    dev_pairs = []
+    for a, b in pairs:
+        da = a.to_device(local)
+        db = da if b is a else b.to_device(local)
+        dev_pairs.append((da, db))
+
+    # bin autotuner (untimed setup): per-bin team shape chosen by measured time on this workload
+    tuned = None
+    if not args.no_tune:
+        da, db = dev_pairs[0]
+        tuned = eng.tune(da, db, reps=2)
+
+    m = device_measure(eng, pairs, dev_pairs, args.steps, args.warmup, local, world)
+    products, c_nnz = m["products"], m["c_nnz"]
+    t_ms, launches, last_phases, clocks = m["t_ms"], m["launches"], m["phases"], m["clocks"]
+    flush, in_bytes = m["flush"], m["in_bytes"]
     t_max = all_max(t_ms, world)
     total_products = all_sum(products * args.steps, world)
     value = 2.0 * total_products / (t_max / 1e3) / 1e9
@@ -410,20 +499,15 @@ def run_gpu_arm(args, rank, world, local):
                   "what": "spg_plan_execute: numeric + scan + compaction of the same products replayed as one "
                           "CUDA graph per step; row work, bins and allocation done once at plan time"}
 
-    pk = peaks()
-    numeric_avg_s = numeric_ms / args.steps / 1e3
-    achieved = bytes_alg / numeric_avg_s / 1e9 if numeric_avg_s > 0 else None
     traffic = None
     tf = ROOT / "profiles" / f"traffic_{args.workload}.json"
-    if tf.exists():
+    if tf.exists() and not args.rows and world == 1:
         traffic = json.loads(tf.read_text()).get("dram_bytes_per_step")
-    roofline = {"bound": "hbm", "kernel": "K4 numeric phase (all bins, one step)", "achieved": achieved,
-                "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": (achieved / pk["hbm_gbs"]) if achieved else None,
-                "peak_source": pk["source"], "traffic": traffic, "bytes_alg": int(bytes_alg),
-                "pipeline_frac": bytes_alg / (t_ms / args.steps / 1e3) / 1e9 / pk["hbm_gbs"]}
+    roofline = dict(m["roofline"])
+    roofline["traffic"] = traffic
 
     cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
         impl, kind = cpu_reference()
         threads = os.cpu_count() or 1
         a, b = pairs[0]
@@ -432,24 +516,34 @@ def run_gpu_arm(args, rank, world, local):
         cpu = {"value": 2.0 * p / t / 1e9, "unit": "GFLOP/s", "cores": threads, "kind": kind,
                "sample": f"rows [{first}, {first + n}) of A x B ({n} of {a.rows} rows, {p} products, {t:.2f} s)"}
 
+    subs = None
+    if rank == 0 and world == 1 and not args.no_sub and args.workload == "powerlaw" and not args.rows:
+        eng.close()
+        eng = None
+        subs = {name: sub_record(name, min(args.steps, 10), args.warmup, local) for name in ("uniform", "galerkin")}
+        subs["batched_subset"] = batched_subset_record(local)
+
     if rank == 0:
         line = {
             "metric": "GFLOP/s", "value": value, "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
+            "scaling": "strong", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "config": {"workload": WORKLOADS[args.workload] + (f" [rows={args.rows}]" if args.rows else ""),
                        "name": args.workload,
                        "products_per_step": int(products), "c_nnz": int(sum(c_nnz)),
                        "l2": ("L2 flushed between timed steps (512 MiB write outside the events)" if flush
                               else f"inputs larger than L2 ({in_bytes / 1e6:.0f} MB, no flush)"),
-                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                       "parallelism": (f"row sharding x{world} (rows cut by the prefix of their scalar products, "
+                                       "B replicated, no collective in the timed region)") if world > 1
+                                      else "single GPU",
                        "bin_variants": tuned["variants"] if tuned else None},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-            "gpu_launches": int(launches), "clocks": clocks.summary(), "graph_replay": replay,
-            "phases_ms_last_step": last_phases,
+            "gpu_launches": int(launches), "clocks": clocks, "graph_replay": replay,
+            "phases_ms_last_step": last_phases, "workloads": subs,
         }
         print(json.dumps(line))
-    eng.close()
+    if eng is not None:
+        eng.close()
 
 
 def _wall(fn):
@@ -697,6 +791,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-replay", action="store_true", help="skip the plan-replay (CUDA graph) sub-measurement")
     ap.add_argument("--no-tune", action="store_true", help="keep the default team shape in every bin")
+    ap.add_argument("--no-sub", action="store_true",
+                    help="skip the uniform, Galerkin and batched-subset records of the default line")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

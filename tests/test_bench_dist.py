@@ -1,7 +1,7 @@
-"""bench.py with several ranks (CPU, gloo, world size 2): the replicas' wall
+"""bench.py with several ranks (CPU, gloo, world size 2): the ranks' wall
 times reduce to the slowest rank and their products to the job total, and the
 reference arm runs on rank 0 only.  No data-path collective exists: each rank
-multiplies its own replica."""
+multiplies its own block of rows."""
 from __future__ import annotations
 
 import os
