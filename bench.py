@@ -246,13 +246,20 @@ def time_cpu_slice(impl, kind: str, a, b, first: int, count: int, threads: int) 
     return time.perf_counter() - t0, products
 
 
-def cpu_sample_rows(impl, kind, a, b, threads: int, target_s: float) -> tuple[int, int]:
-    """A centred row slice sized to take about target_s seconds."""
+CPU_SAMPLE_SECONDS = 8.0   # CPU work per timed reference step (and of the cpu_baseline sample)
+CPU_SAMPLE_QUANTUM = 1 << 17  # sample sizes are whole multiples of this many rows (or all rows)
+
+
+def cpu_sample_rows(impl, kind, a, b, threads: int, target_s: float = CPU_SAMPLE_SECONDS) -> tuple[int, int]:
+    """A centred row slice sized to take about target_s seconds, rounded up to a
+    multiple of CPU_SAMPLE_QUANTUM rows (all rows when that covers A), so that
+    the reference arm and the GPU arm's cpu_baseline time the same rows."""
     m = a.rows
     n = min(m, 2048)
     first = max(0, m // 2 - n // 2)
     t, _ = time_cpu_slice(impl, kind, a, b, first, n, threads)
-    n = int(min(m, max(n, n * target_s / max(t, 1e-6))))
+    want = n * target_s / max(t, 1e-6)
+    n = int(min(m, -(-max(want, 1) // CPU_SAMPLE_QUANTUM) * CPU_SAMPLE_QUANTUM))
     first = max(0, m // 2 - n // 2)
     return first, n
 
@@ -263,9 +270,8 @@ def run_reference_arm(args, rank, world):
     pairs = make_workload(args.workload, args.rows)
     impl, kind = cpu_reference()
     threads = os.cpu_count() or 1
-    per_step = max(1.0, args.reference_step_seconds)
     a, b = pairs[0]
-    first, n = cpu_sample_rows(impl, kind, a, b, threads, per_step)
+    first, n = cpu_sample_rows(impl, kind, a, b, threads)
     for _ in range(args.warmup):
         time_cpu_slice(impl, kind, a, b, first, n, threads)
     tot_t, tot_p = 0.0, 0
@@ -511,7 +517,7 @@ def run_gpu_arm(args, rank, world, local):
         impl, kind = cpu_reference()
         threads = os.cpu_count() or 1
         a, b = pairs[0]
-        first, n = cpu_sample_rows(impl, kind, a, b, threads, args.cpu_seconds)
+        first, n = cpu_sample_rows(impl, kind, a, b, threads)
         t, p = time_cpu_slice(impl, kind, a, b, first, n, threads)
         cpu = {"value": 2.0 * p / t / 1e9, "unit": "GFLOP/s", "cores": threads, "kind": kind,
                "sample": f"rows [{first}, {first + n}) of A x B ({n} of {a.rows} rows, {p} products, {t:.2f} s)"}
@@ -784,8 +790,6 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="powerlaw")
     ap.add_argument("--rows", type=int, default=0, help="power-law rows (default 1048576; profiling only)")
-    ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--reference-step-seconds", type=float, default=8.0)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -427,84 +427,92 @@ void run_products(spg_handle* h, const std::vector<JobIn>& in, std::vector<DevRe
         throw Failure{s, msg};
     }
     const int64_t nz_total = static_cast<int64_t>(hc->stats.nz_total);
-    int64_t* final_rp = cnt;
-    int32_t* final_col = c_col;
-    double* final_val = c_val;
-    if (nz_total != tmp_total) {  // rows with fewer entries than reserved: compact
-        launch_scan(nz, static_cast<int64_t>(slots) - 1, partials, st);
-        launches += 3 + (exact ? njobs : 1);
-        final_col = ar.alloc<int32_t>(static_cast<size_t>(nz_total), "C col (compact)");
-        final_val = ar.alloc<double>(static_cast<size_t>(nz_total), "C val (compact)");
-        if (exact) {
-            for (int j = 0; j < njobs; ++j) launch_compact(d_jobs + j, in[j].A->rows, final_col, final_val, st);
-        } else {
-            launch_compact_holes(d_jobs, njobs, d_row_base, total_rows, final_col, final_val, st);
+    out.resize(njobs);
+    if (njobs == 1) {
+        int64_t* final_rp = cnt;
+        int32_t* final_col = c_col;
+        double* final_val = c_val;
+        if (nz_total != tmp_total) {  // rows with fewer entries than reserved: compact
+            launch_scan(nz, static_cast<int64_t>(slots) - 1, partials, st);
+            launches += 4;
+            final_col = ar.alloc<int32_t>(static_cast<size_t>(nz_total), "C col (compact)");
+            final_val = ar.alloc<double>(static_cast<size_t>(nz_total), "C val (compact)");
+            if (exact) launch_compact(d_jobs, in[0].A->rows, final_col, final_val, st);
+            else launch_compact_holes(d_jobs, 1, d_row_base, total_rows, final_col, final_val, st);
+            check_cuda(cudaGetLastError(), "K5 launch");
+            final_rp = nz;
+            ar.free_now(c_col);
+            ar.free_now(c_val);
         }
-        check_cuda(cudaGetLastError(), "K5 launch");
-        final_rp = nz;
-        ar.free_now(c_col);
-        ar.free_now(c_val);
-    }
-    cudaEventRecord(h->ev[5], st);
-
-    // results: offsets of job j start at final_rp[row_base_j + j]
-    std::vector<int64_t> starts(njobs + 1, 0);
-    starts[njobs] = nz_total;
-    if (njobs > 1) {
+        cudaEventRecord(h->ev[5], st);
+        DevResult& r = out[0];
+        r.rows = in[0].A->rows;
+        r.cols = in[0].B->cols;
+        r.nnz = nz_total;
+        r.rp = final_rp;
+        r.ci = final_col;
+        r.v = final_val;
+        ar.release(final_rp);
+        ar.release(final_col);
+        ar.release(final_val);
+    } else {
+        // Every product gets arrays of its own, which the compaction fills
+        // directly (row r of product j at its offset minus the product's first
+        // offset): the entries of C are moved once, not compacted and then
+        // copied out of one flat array.
+        launch_scan(nz, static_cast<int64_t>(slots) - 1, partials, st);
         std::vector<int64_t> idx(njobs);
         for (int j = 0; j < njobs; ++j) idx[j] = row_base[j] + j;
         int64_t* d_idx = ar.alloc<int64_t>(static_cast<size_t>(njobs), "start index");
         int64_t* d_starts = ar.alloc<int64_t>(static_cast<size_t>(njobs), "starts");
         check_cuda(cudaMemcpyAsync(d_idx, idx.data(), sizeof(int64_t) * njobs, cudaMemcpyHostToDevice, st),
                    "H2D start index");
-        launch_gather(final_rp, d_idx, d_starts, njobs, st);
+        launch_gather(nz, d_idx, d_starts, njobs, st);
         int64_t* h_starts = static_cast<int64_t*>(host_staging(h, sizeof(int64_t) * njobs));
         launch_readback(d_starts, h_starts, sizeof(int64_t) * njobs, st);
-        launches += 3;  // gather + readback + rebase
-        sync(h);
-        std::copy(h_starts, h_starts + njobs, starts.begin());
-    }
-    out.resize(njobs);
-    for (int j = 0; j < njobs; ++j) {
-        DevResult& r = out[j];
-        r.rows = in[j].A->rows;
-        r.cols = in[j].B->cols;
-        r.nnz = starts[j + 1] - starts[j];
-        if (njobs == 1) {
-            r.rp = final_rp;
-            r.ci = final_col;
-            r.v = final_val;
-            ar.release(final_rp);
-            ar.release(final_col);
-            ar.release(final_val);
-        } else {
-            r.rp = ar.alloc<int64_t>(static_cast<size_t>(r.rows) + 1, "result row_ptr");
-            r.ci = ar.alloc<int32_t>(static_cast<size_t>(r.nnz), "result col");
-            r.v = ar.alloc<double>(static_cast<size_t>(r.nnz), "result val");
-            check_cuda(cudaMemcpyAsync(r.ci, final_col + starts[j], sizeof(int32_t) * r.nnz, cudaMemcpyDeviceToDevice, st),
-                       "D2D col");
-            check_cuda(cudaMemcpyAsync(r.v, final_val + starts[j], sizeof(double) * r.nnz, cudaMemcpyDeviceToDevice, st),
-                       "D2D val");
-            check_cuda(cudaMemcpyAsync(r.rp, final_rp + row_base[j] + j, sizeof(int64_t) * (r.rows + 1),
-                                       cudaMemcpyDeviceToDevice, st), "D2D row_ptr");
-            ar.release(r.rp);
-            ar.release(r.ci);
-            ar.release(r.v);
-        }
-    }
-    if (njobs > 1) {  // every product's offsets start at zero
+        launches += 5;
+        sync(h);  // every product's first offset: the sizes of its arrays
+        std::vector<int64_t> starts(h_starts, h_starts + njobs);
+        starts.push_back(nz_total);
         std::vector<RebaseItem> rb(njobs);
         int64_t max_rows = 0;
         for (int j = 0; j < njobs; ++j) {
-            rb[j] = RebaseItem{out[j].rp, starts[j], out[j].rows};
-            max_rows = std::max<int64_t>(max_rows, out[j].rows);
+            DevResult& r = out[j];
+            r.rows = in[j].A->rows;
+            r.cols = in[j].B->cols;
+            r.nnz = starts[j + 1] - starts[j];
+            r.rp = ar.alloc<int64_t>(static_cast<size_t>(r.rows) + 1, "result row_ptr");
+            r.ci = ar.alloc<int32_t>(static_cast<size_t>(r.nnz), "result col");
+            r.v = ar.alloc<double>(static_cast<size_t>(r.nnz), "result val");
+            jobs[j].out_col = r.ci;
+            jobs[j].out_val = r.v;
+            check_cuda(cudaMemcpyAsync(r.rp, nz + row_base[j] + j, sizeof(int64_t) * (r.rows + 1),
+                                       cudaMemcpyDeviceToDevice, st), "D2D row_ptr");
+            rb[j] = RebaseItem{r.rp, starts[j], r.rows};
+            max_rows = std::max<int64_t>(max_rows, r.rows);
         }
+        check_cuda(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(Job) * njobs, cudaMemcpyHostToDevice, st), "H2D jobs");
+        if (exact) {
+            for (int j = 0; j < njobs; ++j) launch_compact(d_jobs + j, in[j].A->rows, nullptr, nullptr, st);
+        } else {
+            launch_compact_holes(d_jobs, njobs, d_row_base, total_rows, nullptr, nullptr, st);
+        }
+        check_cuda(cudaGetLastError(), "K5 launch");
+        ar.free_now(c_col);
+        ar.free_now(c_val);
+        cudaEventRecord(h->ev[5], st);
         RebaseItem* d_rb = ar.alloc<RebaseItem>(static_cast<size_t>(njobs), "rebase items");
         check_cuda(cudaMemcpyAsync(d_rb, rb.data(), sizeof(RebaseItem) * njobs, cudaMemcpyHostToDevice, st),
                    "H2D rebase");
         launch_rebase(d_rb, njobs, max_rows, st);
         check_cuda(cudaGetLastError(), "rebase launch");
-        sync(h);  // rb / idx host vectors must outlive the copies
+        launches += 2 + (exact ? njobs : 1);
+        for (auto& r : out) {
+            ar.release(r.rp);
+            ar.release(r.ci);
+            ar.release(r.v);
+        }
+        sync(h);  // jobs, idx and rb must outlive their copies
     }
     for (int j = 0; j < njobs; ++j) out[j].products = job_products[j];
     sync(h);

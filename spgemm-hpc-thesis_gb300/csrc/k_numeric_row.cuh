@@ -55,6 +55,16 @@ __device__ __forceinline__ int hidx(int d, int w) {
     return W == 1 ? d : d * kHistStride<W> + w;
 }
 
+// Bucket sort of CTA rows (bucket_sort below): 2^kCoarseBits coarse buckets,
+// whose 16-bit counters take kBkCoarseWords words and whose table (first fine
+// bucket, fine bits) kBkInfoWords; then at most one fine counter per product.
+constexpr int kCoarseBits = 8;
+constexpr int kBkCoarseWords = (1 << kCoarseBits) / 2;
+constexpr int kBkInfoWords = 1 << kCoarseBits;
+// A fine bucket holding more products than this (a column repeated many times)
+// sends the row to the radix sort: ranking inside a bucket is quadratic.
+constexpr uint32_t kMaxFine = 64;
+
 // SV: product values in shared memory (else in a per-CTA global slab).
 template <int W, int ITEMS, bool SV = true>
 struct RowSmem {
@@ -64,9 +74,15 @@ struct RowSmem {
     SegTab<W * 32, int32_t> seg;  // enumeration batch
     int64_t warp_tmp[W + 1];    // block scans
     uint32_t keys[kCap];        // columns (unpacked) or packed (column, sequence) words
-    alignas(16) uint32_t hist[W == 1 ? 1 : 2][kHistWords<W>];  // digit counters at hidx<W>(digit, warp); CTA rows
-                                                   // alternate two sets so that clearing the next
-                                                   // pass's set needs no barrier of its own
+    union {
+        // digit counters of the radix sort at hidx<W>(digit, warp); CTA rows
+        // alternate two sets so that clearing the next pass's set needs no
+        // barrier of its own
+        alignas(16) uint32_t hist[W == 1 ? 1 : 2][kHistWords<W>];
+        // bucket sort of CTA rows: coarse counters, coarse bucket table, fine
+        // counters (16-bit counters, two per word)
+        alignas(16) uint32_t bk[W == 1 ? 1 : kBkCoarseWords + kBkInfoWords + kCap / 2 + 1];
+    };
     uint32_t cnt[W * ITEMS];    // kept entries per (warp, item)
     uint16_t seqs[kCap];        // sequence numbers of the unpacked path
     int32_t red[2 * W];         // min / max column reduction
@@ -176,6 +192,223 @@ __device__ inline void scan_kept(uint32_t* cnt, int32_t* red, int warp, int lane
     }
 }
 
+// 16-bit counter i of an array of packed pairs (low half: even i).
+__device__ __forceinline__ uint32_t half16(const uint32_t* a, uint32_t i) {
+    return (a[i >> 1] >> ((i & 1u) << 4)) & 0xffffu;
+}
+// Adds one to 16-bit counter i and returns its previous value.
+__device__ __forceinline__ uint32_t bump16(uint32_t* a, uint32_t i) {
+    const uint32_t sh = (i & 1u) << 4;
+    return (atomicAdd(&a[i >> 1], 1u << sh) >> sh) & 0xffffu;
+}
+// bump16 for every valid lane of a warp (all 32 lanes call it), one atomic per
+// run of consecutive lanes with the same counter: consecutive products of one
+// B row mostly fall into the same coarse bucket, and a shared atomic that many
+// lanes aim at one word is serialised.  Valid lanes are a prefix of the warp.
+__device__ __forceinline__ void bump16_runs(uint32_t* a, uint32_t i, bool valid, int lane) {
+    const uint32_t prev = __shfl_up_sync(0xffffffffu, i, 1);
+    const bool head = valid && (lane == 0 || prev != i);
+    const unsigned heads = __ballot_sync(0xffffffffu, head);
+    const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+    if (head) {
+        const unsigned later = heads & ~((2u << lane) - 1u);  // heads after this lane (lane 31: none)
+        const int next = later ? __ffs(later) - 1 : __popc(vmask);
+        atomicAdd(&a[i >> 1], static_cast<uint32_t>(next - lane) << ((i & 1u) << 4));
+    }
+}
+
+// Exclusive scan of v over the W*32 threads of a CTA in thread order, with the
+// total and the CTA-wide maximum of m (red: 2*W words; two barriers).
+template <int W>
+__device__ inline uint32_t block_excl_scan_max(uint32_t v, uint32_t m, int32_t* red, int lane, int warp,
+                                               uint32_t& total, uint32_t& mx) {
+    const uint32_t incl = warp_incl_scan(v, lane);
+    const uint32_t wm = warp_max(m);
+    if (lane == 31) {
+        red[warp] = static_cast<int32_t>(incl);
+        red[W + warp] = static_cast<int32_t>(wm);
+    }
+    __syncthreads();
+    uint32_t base = 0, tot = 0, gm = 0;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        const uint32_t s = static_cast<uint32_t>(red[w]);
+        base += w < warp ? s : 0u;
+        tot += s;
+        gm = max(gm, static_cast<uint32_t>(red[W + w]));
+    }
+    __syncthreads();
+    total = tot;
+    mx = gm;
+    return base + incl - v;
+}
+
+// Step 2 of a CTA row without digit passes: the products (columns at
+// keys[0..P), offsets k = column - cmin of nbits >= 1 bits, sequence number =
+// position) are bucketed, then ranked inside their bucket.
+//   * coarse buckets: the top min(nbits, 8) bits of k (16-bit counters);
+//   * coarse bucket c of n_c products gets 2^fb_c fine buckets over its column
+//     span, fb_c = min(span bits, floor(log2 n_c)), so that dense parts of the
+//     row (the diagonal band of a banded product) get finer buckets than sparse
+//     ones and no more fine buckets than products exist;
+//   * the products are scattered into their fine buckets in any order (shared
+//     atomics), then every product finds its place in its bucket by counting
+//     the bucket's products with a smaller (column, sequence) pair: the pair is
+//     unique, so the result is the order of a stable sort by column, the
+//     reference's order of every column's products.
+// Instruction cost per product does not grow with the column range, unlike a
+// digit pass.  Returns false, leaving keys untouched, when a fine bucket would
+// hold more than kMaxFine products (a column repeated that often); the row then
+// takes the radix sort.  On success keys (and seqs when !PACKED) hold the sorted
+// products in the layout finish_row reads: packed (column - cmin, sequence)
+// words, or columns and 16-bit sequence numbers side by side.
+template <int W, int ITEMS, bool SV, bool PACKED>
+__device__ bool bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int nbits, int lane, int warp,
+                            int tid) {
+    using Sm = RowSmem<W, ITEMS, SV>;
+    constexpr int NT = W * 32;
+    constexpr int kSeqBits = Sm::kSeqBits;
+    static_assert(sizeof(sm.bk) <= sizeof(sm.hist), "bucket counters share the radix counters' space");
+    uint32_t* cc = sm.bk;                                     // coarse counters
+    uint32_t* info = sm.bk + kBkCoarseWords;                  // first fine bucket | fine bits << 16
+    uint32_t* fc = sm.bk + kBkCoarseWords + kBkInfoWords;     // fine counters, then starts, then ends
+    const int cbits = nbits < kCoarseBits ? nbits : kCoarseBits;
+    const int sc = nbits - cbits;                             // column bits inside a coarse bucket
+    const uint32_t scmask = (1u << sc) - 1u;
+    // 0. clear the coarse counters and enough fine counters for P products
+    const int fwords = (P + 1) >> 1;
+    for (int i = tid; i < kBkCoarseWords; i += NT) cc[i] = 0u;
+    for (int i = tid; i < fwords; i += NT) fc[i] = 0u;
+    __syncthreads();
+    // 1. coarse histogram
+    uint32_t k[ITEMS], f[ITEMS];
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+        const int pos = (warp * ITEMS + i) * 32 + lane;
+        k[i] = pos < P ? sm.keys[pos] - cmin : 0u;
+        bump16_runs(cc, k[i] >> sc, pos < P, lane);
+    }
+    __syncthreads();
+    // 2. fine buckets of every coarse bucket, numbered in coarse order (one
+    //    warp: eight coarse buckets per lane)
+    if (warp == 0) {
+        constexpr int kPer = (1 << kCoarseBits) / 32;
+        uint32_t fcount[kPer], fbits[kPer], sum = 0;
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            const uint32_t n = half16(cc, static_cast<uint32_t>(lane * kPer + j));  // zero beyond 2^cbits
+            const int lg = n ? 31 - __clz(n) : 0;
+            fbits[j] = static_cast<uint32_t>(lg < sc ? lg : sc);
+            fcount[j] = n ? (1u << fbits[j]) : 0u;
+            sum += fcount[j];
+        }
+        uint32_t base = warp_incl_scan(sum, lane) - sum;
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            info[lane * kPer + j] = base | (fbits[j] << 16);
+            base += fcount[j];
+        }
+    }
+    __syncthreads();
+    // 3. fine histogram
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+        const int pos = (warp * ITEMS + i) * 32 + lane;
+        f[i] = 0u;
+        if (pos < P) {
+            const uint32_t in = info[k[i] >> sc];
+            f[i] = (in & 0xffffu) + ((k[i] & scmask) >> (sc - static_cast<int>(in >> 16)));
+            bump16(fc, f[i]);
+        }
+    }
+    __syncthreads();
+    // 4. exclusive scan of the fine counters (at most P of them; contiguous
+    //    words per thread), and the largest fine bucket
+    {
+        const int per = (fwords + NT - 1) / NT;
+        const int w0 = tid * per;
+        const int w1 = min(w0 + per, fwords);
+        uint32_t sum = 0, mx = 0;
+        for (int w = w0; w < w1; ++w) {
+            const uint32_t x = fc[w];
+            const uint32_t lo = x & 0xffffu, hi = x >> 16;
+            sum += lo + hi;
+            mx = max(mx, max(lo, hi));
+        }
+        uint32_t total, gmax;
+        uint32_t base = block_excl_scan_max<W>(sum, mx, sm.red, lane, warp, total, gmax);
+        if (gmax > kMaxFine) return false;  // uniform: every thread saw the same maximum
+        for (int w = w0; w < w1; ++w) {
+            const uint32_t x = fc[w];
+            const uint32_t lo = x & 0xffffu;
+            fc[w] = base | ((base + lo) << 16);
+            base += lo + (x >> 16);
+        }
+    }
+    __syncthreads();
+    // 5. scatter into the fine buckets (any order inside a bucket)
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+        const int pos = (warp * ITEMS + i) * 32 + lane;
+        if (pos < P) {
+            const uint32_t at = bump16(fc, f[i]);
+            if constexpr (PACKED) {
+                sm.keys[at] = (k[i] << kSeqBits) | static_cast<uint32_t>(pos);
+            } else {
+                sm.keys[at] = k[i] + cmin;  // the unpacked layout keeps columns
+                sm.seqs[at] = static_cast<uint16_t>(pos);
+            }
+        }
+    }
+    __syncthreads();
+    // 6. every sorted position takes its product's place inside the product's
+    //    bucket: the number of the bucket's products with a smaller (column,
+    //    sequence) pair.  Positions run in lane order, so the lanes of a warp
+    //    mostly share buckets (same loop bounds, broadcast loads).  The counters
+    //    now hold every bucket's end.
+    uint32_t* const dst = f;  // the fine indices are no longer needed
+    uint32_t* const key = k;  // nor the column offsets
+    uint32_t sqv[PACKED ? 1 : ITEMS];  // sequence numbers of the unpacked layout
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+        const int p = (warp * ITEMS + i) * 32 + lane;
+        key[i] = 0u;
+        dst[i] = 0u;
+        if (p < P) {
+            key[i] = sm.keys[p];
+            const uint32_t kk = PACKED ? key[i] >> kSeqBits : key[i] - cmin;
+            const uint32_t in = info[kk >> sc];
+            const uint32_t fb = (in & 0xffffu) + ((kk & scmask) >> (sc - static_cast<int>(in >> 16)));
+            const uint32_t end = half16(fc, fb);
+            const uint32_t beg = fb ? half16(fc, fb - 1u) : 0u;
+            uint32_t r = 0;
+            if constexpr (PACKED) {
+                for (uint32_t q = beg; q < end; ++q) r += sm.keys[q] < key[i] ? 1u : 0u;
+            } else {
+                const uint32_t sq = sm.seqs[p];
+                for (uint32_t q = beg; q < end; ++q) {
+                    const uint32_t kq = sm.keys[q];
+                    r += (kq < key[i] || (kq == key[i] && sm.seqs[q] < sq)) ? 1u : 0u;
+                }
+                sqv[i] = sq;
+            }
+            dst[i] = beg + r;
+        }
+    }
+    __syncthreads();
+    // 7. products at their sorted positions
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+        const int p = (warp * ITEMS + i) * 32 + lane;
+        if (p < P) {
+            sm.keys[dst[i]] = key[i];
+            if constexpr (!PACKED) sm.seqs[dst[i]] = static_cast<uint16_t>(sqv[i]);
+        }
+    }
+    __syncthreads();
+    return true;
+}
+
 // Where a row's result goes, read once from the Job (locals, not reloaded
 // through the Job reference after every global store).
 struct RowOut {
@@ -187,17 +420,16 @@ struct RowOut {
     int32_t nz_add;     // a piece of a split row: add to *nz instead of storing it
 };
 
-// Steps 2-4 of a row for one key layout (PACKED: (col - cmin) << kSeqBits | seq
-// words; otherwise columns and 16-bit sequence numbers).
-template <int W, int ITEMS, bool SV, bool PACKED>
-__device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double* vals, int P, uint32_t cmin,
-                           int nbits, int lane, int warp, int tid) {
-    using Sm = RowSmem<W, ITEMS, SV>;
-    constexpr int kSeqBits = Sm::kSeqBits;
-    // 2. stable LSD radix sort by column: 8-bit digits, and a last pass of at
-    //    most 4 bits (four votes, 16 counters per warp) when no more remain
+// The stable LSD radix sort of a row's products by column: 8-bit digits over
+// the bits of max(col) - min(col), and with kNarrow a last pass of at most 4
+// bits (four votes, 16 counters per warp) when no more remain.  Leaves keys
+// (and seqs when !PACKED) in the layout finish_row reads.
+template <int W, int ITEMS, bool SV, bool PACKED, bool kNarrow>
+__device__ __forceinline__ void radix_sort_row(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int nbits, int lane,
+                                               int warp, int tid) {
+    constexpr int kSeqBits = RowSmem<W, ITEMS, SV>::kSeqBits;
     int hb = 0;  // counter set of this pass
-    auto digits_from = [&](int shift) { return nbits - shift > 4 ? 256 : 16; };
+    auto digits_from = [&](int shift) { return (kNarrow && nbits - shift <= 4) ? 16 : 256; };
     if constexpr (PACKED) {
         if (nbits == 0) {  // one column: already in sequence order; just pack
 #pragma unroll
@@ -271,11 +503,11 @@ __device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double*
         }
     };
     for (int shift = 0; shift < nbits;) {
-        if (nbits - shift > 4) {
+        if (!kNarrow || nbits - shift > 4) {
             pass(std::integral_constant<int, 8>{}, shift);
             shift += 8;
         } else {
-            pass(std::integral_constant<int, 4>{}, shift);
+            if constexpr (kNarrow) pass(std::integral_constant<int, 4>{}, shift);
             shift += 4;
         }
         const bool more = shift < nbits;
@@ -287,6 +519,41 @@ __device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double*
             hb ^= 1;
         }
         row_sync<W>();
+    }
+
+}
+
+// The radix sort of CTA rows that the bucket sort declined (a column repeated
+// more than kMaxFine times): rare, so it keeps the code small rather than fast
+// -- one key layout (columns and sequence numbers) and 8-bit digits only, then
+// the packed words when the row's layout is packed.  Less code in the CTA
+// kernels measured 0.25 ms faster on the power-law product than the full radix
+// sort inline.
+template <int W, int ITEMS, bool SV, bool PACKED>
+__device__ __forceinline__ void radix_sort_fallback(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int nbits,
+                                                    int lane, int warp, int tid) {
+    constexpr int kSeqBits = RowSmem<W, ITEMS, SV>::kSeqBits;
+    radix_sort_row<W, ITEMS, SV, false, false>(sm, P, cmin, nbits, lane, warp, tid);
+    if constexpr (PACKED) {
+        for (int i = tid; i < P; i += W * 32) sm.keys[i] = ((sm.keys[i] - cmin) << kSeqBits) | sm.seqs[i];
+        __syncthreads();
+    }
+}
+
+// Steps 2-4 of a row for one key layout (PACKED: (col - cmin) << kSeqBits | seq
+// words; otherwise columns and 16-bit sequence numbers).
+template <int W, int ITEMS, bool SV, bool PACKED>
+__device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double* vals, int P, uint32_t cmin,
+                           int nbits, int lane, int warp, int tid) {
+    using Sm = RowSmem<W, ITEMS, SV>;
+    constexpr int kSeqBits = Sm::kSeqBits;
+    // 2. sort by column: the bucket sort for CTA rows, the radix sort for warp
+    //    rows and where the bucket sort declines
+    if constexpr (W == 1) {
+        radix_sort_row<W, ITEMS, SV, PACKED, true>(sm, P, cmin, nbits, lane, warp, tid);
+    } else {
+        if (nbits == 0 || !bucket_sort<W, ITEMS, SV, PACKED>(sm, P, cmin, nbits, lane, warp, tid))
+            radix_sort_fallback<W, ITEMS, SV, PACKED>(sm, P, cmin, nbits, lane, warp, tid);
     }
 
     // Column and sequence number of sorted position pos.

@@ -214,10 +214,18 @@ compact_kernel(const Job* __restrict__ job, int rows, int32_t* __restrict__ out_
     const int lane = threadIdx.x & 31;
     const int64_t warps = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
     for (int64_t r = static_cast<int64_t>(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5); r < rows; r += warps) {
-        const int64_t src = job->cnt[r], dst = job->nz[r], n = job->nz[r + 1] - dst;
+        const int64_t src = job->cnt[r], n = job->nz[r + 1] - job->nz[r];
+        int32_t* oc = out_col;
+        double* ov = out_val;
+        int64_t dst = job->nz[r];
+        if (!oc) {  // the job's own arrays
+            oc = job->out_col;
+            ov = job->out_val;
+            dst -= job->nz[0];
+        }
         for (int64_t q = lane; q < n; q += 32) {
-            out_col[dst + q] = job->c_col[src + q];
-            out_val[dst + q] = job->c_val[src + q];
+            oc[dst + q] = job->c_col[src + q];
+            ov[dst + q] = job->c_val[src + q];
         }
     }
 }
@@ -242,11 +250,13 @@ compact_holes_kernel(const Job* __restrict__ jobs, int njobs, const int64_t* __r
         const int r = static_cast<int>(row - job_row_base[j]);
         n_src = jobs[j].cnt[r];
         n_end = jobs[j].cnt[r + 1];
-        n_dst = jobs[j].nz[r];
+        n_dst = jobs[j].nz[r] - (out_col ? 0 : jobs[j].nz[0]);  // the job's own arrays start at its first row
     };
     if (g < total_rows) load_row(g);
     for (; g < total_rows; g += warps) {
         const Job& J = jobs[j];
+        int32_t* __restrict__ oc = out_col ? out_col : J.out_col;
+        double* __restrict__ ov = out_col ? out_val : J.out_val;
         const int64_t src = n_src, end = n_end;
         int64_t dst = n_dst;
         if (g + warps < total_rows) load_row(g + warps);
@@ -266,8 +276,8 @@ compact_holes_kernel(const Job* __restrict__ jobs, int njobs, const int64_t* __r
                 const unsigned m = __ballot_sync(0xffffffffu, c[u] >= 0);
                 if (c[u] >= 0) {
                     const int64_t at = dst + __popc(m & lanemask_lt());
-                    out_col[at] = c[u];
-                    out_val[at] = v[u];
+                    oc[at] = c[u];
+                    ov[at] = v[u];
                 }
                 dst += __popc(m);
             }

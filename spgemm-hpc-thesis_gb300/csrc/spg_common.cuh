@@ -39,6 +39,8 @@ struct Job {
     int64_t row_base = 0;     // first flattened row of this job in a batch
     int32_t holes = 0;        // 1: rows are written slot by slot into their reserved C_tmp range,
                               // column -1 marking unused slots (upper-bound mode); 0: compacted
+    int32_t* out_col = nullptr;  // this product's own result arrays (a batch): K5 writes row r at
+    double* out_val = nullptr;   // nz[r] - nz[0]; else K5 writes into the arrays it is given
 };
 
 // Row bins by product count (ub): capacities 32, 64, then two per power of two
@@ -223,7 +225,8 @@ inline SplitTotals split_totals(const Stats& st) {
     return SplitTotals{static_cast<int64_t>(st.split_products),
                        static_cast<int64_t>(st.bin_count[17] + st.bin_count[18] + st.bin_count[kBinHeavy])};
 }
-// K5: move rows from C_tmp (offsets job.cnt) to C (offsets job.nz, scanned).
+// K5: move rows from C_tmp (offsets job.cnt) to C (offsets job.nz, scanned);
+// with out_col == nullptr, into the job's own arrays (Job::out_col / out_val).
 void launch_compact(const Job* d_job, int rows, int32_t* out_col, double* out_val, cudaStream_t stream);
 // K5 for rows written with holes: keeps the slots whose column is >= 0.
 void launch_compact_holes(const Job* d_jobs, int njobs, const int64_t* d_job_row_base, int64_t total_rows,
