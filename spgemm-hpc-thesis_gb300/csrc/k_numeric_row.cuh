@@ -55,12 +55,28 @@ __device__ __forceinline__ int hidx(int d, int w) {
     return W == 1 ? d : d * kHistStride<W> + w;
 }
 
-// Bucket sort of CTA rows (bucket_sort below): 2^kCoarseBits coarse buckets,
-// whose 16-bit counters take kBkCoarseWords words and whose table (first fine
-// bucket, fine bits) kBkInfoWords; then at most one fine counter per product.
-constexpr int kCoarseBits = 8;
-constexpr int kBkCoarseWords = (1 << kCoarseBits) / 2;
-constexpr int kBkInfoWords = 1 << kCoarseBits;
+// Bucket sort (bucket_sort below): 2^kCoarseBits<W> coarse buckets, whose
+// 16-bit counters take kBkCoarseWords<W> words and whose table (first fine
+// bucket, fine bits) kBkInfoWords<W>; then at most one fine counter per
+// product.  Warp rows take 32 coarse buckets, so that the counters fit the
+// space of their radix counters.
+template <int W>
+constexpr int kCoarseBits = W == 1 ? 5 : 8;
+template <int W>
+constexpr int kBkCoarseWords = (1 << kCoarseBits<W>) / 2;
+template <int W>
+constexpr int kBkInfoWords = 1 << kCoarseBits<W>;
+template <int W, int ITEMS>
+constexpr int kBkWords = kBkCoarseWords<W> + kBkInfoWords<W> + W * 32 * ITEMS / 2 + 1;
+// Warp rows of at least this many products per lane take the bucket sort
+// where its counters fit (up to 12 per lane); smaller ones the radix sort.
+constexpr int kWarpBucketItems = 3;
+// In the packed layout the scatter also stores every product's fine bucket
+// beside it (in the sequence-number array, which that layout leaves unused),
+// so that ranking a position reads its bucket instead of recomputing it.
+constexpr bool kStoreFine = true;
+template <int W, int ITEMS>
+constexpr bool kBucketRows = W > 1 || (ITEMS >= kWarpBucketItems && kBkWords<1, ITEMS> <= kHistWords<1>);
 // A fine bucket holding more products than this (a column repeated many times)
 // sends the row to the radix sort: ranking inside a bucket is quadratic.
 constexpr uint32_t kMaxFine = 64;
@@ -81,7 +97,7 @@ struct RowSmem {
         alignas(16) uint32_t hist[W == 1 ? 1 : 2][kHistWords<W>];
         // bucket sort of CTA rows: coarse counters, coarse bucket table, fine
         // counters (16-bit counters, two per word)
-        alignas(16) uint32_t bk[W == 1 ? 1 : kBkCoarseWords + kBkInfoWords + kCap / 2 + 1];
+        alignas(16) uint32_t bk[kBucketRows<W, ITEMS> ? kBkWords<W, ITEMS> : 1];
     };
     uint32_t cnt[W * ITEMS];    // kept entries per (warp, item)
     uint16_t seqs[kCap];        // sequence numbers of the unpacked path
@@ -217,13 +233,19 @@ __device__ __forceinline__ void bump16_runs(uint32_t* a, uint32_t i, bool valid,
     }
 }
 
-// Exclusive scan of v over the W*32 threads of a CTA in thread order, with the
-// total and the CTA-wide maximum of m (red: 2*W words; two barriers).
+// Exclusive scan of v over the W*32 threads of a row's team in thread order,
+// with the total and the team-wide maximum of m (red: 2*W words; two barriers
+// for a CTA, none for a warp).
 template <int W>
 __device__ inline uint32_t block_excl_scan_max(uint32_t v, uint32_t m, int32_t* red, int lane, int warp,
                                                uint32_t& total, uint32_t& mx) {
     const uint32_t incl = warp_incl_scan(v, lane);
     const uint32_t wm = warp_max(m);
+    if constexpr (W == 1) {
+        total = __shfl_sync(0xffffffffu, incl, 31);
+        mx = wm;
+        return incl - v;
+    }
     if (lane == 31) {
         red[warp] = static_cast<int32_t>(incl);
         red[W + warp] = static_cast<int32_t>(wm);
@@ -268,18 +290,19 @@ __device__ bool bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int
     using Sm = RowSmem<W, ITEMS, SV>;
     constexpr int NT = W * 32;
     constexpr int kSeqBits = Sm::kSeqBits;
+    static_assert(kBucketRows<W, ITEMS>, "rows of this shape have no bucket counters");
     static_assert(sizeof(sm.bk) <= sizeof(sm.hist), "bucket counters share the radix counters' space");
     uint32_t* cc = sm.bk;                                     // coarse counters
-    uint32_t* info = sm.bk + kBkCoarseWords;                  // first fine bucket | fine bits << 16
-    uint32_t* fc = sm.bk + kBkCoarseWords + kBkInfoWords;     // fine counters, then starts, then ends
-    const int cbits = nbits < kCoarseBits ? nbits : kCoarseBits;
+    uint32_t* info = sm.bk + kBkCoarseWords<W>;                  // first fine bucket | fine bits << 16
+    uint32_t* fc = sm.bk + kBkCoarseWords<W> + kBkInfoWords<W>;     // fine counters, then starts, then ends
+    const int cbits = nbits < kCoarseBits<W> ? nbits : kCoarseBits<W>;
     const int sc = nbits - cbits;                             // column bits inside a coarse bucket
     const uint32_t scmask = (1u << sc) - 1u;
     // 0. clear the coarse counters and enough fine counters for P products
     const int fwords = (P + 1) >> 1;
-    for (int i = tid; i < kBkCoarseWords; i += NT) cc[i] = 0u;
+    for (int i = tid; i < kBkCoarseWords<W>; i += NT) cc[i] = 0u;
     for (int i = tid; i < fwords; i += NT) fc[i] = 0u;
-    __syncthreads();
+    row_sync<W>();
     // 1. coarse histogram
     uint32_t k[ITEMS], f[ITEMS];
 #pragma unroll
@@ -288,11 +311,11 @@ __device__ bool bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int
         k[i] = pos < P ? sm.keys[pos] - cmin : 0u;
         bump16_runs(cc, k[i] >> sc, pos < P, lane);
     }
-    __syncthreads();
+    row_sync<W>();
     // 2. fine buckets of every coarse bucket, numbered in coarse order (one
-    //    warp: eight coarse buckets per lane)
+    //    warp)
     if (warp == 0) {
-        constexpr int kPer = (1 << kCoarseBits) / 32;
+        constexpr int kPer = (1 << kCoarseBits<W>) / 32;  // 8 for CTA rows, 1 for warp rows
         uint32_t fcount[kPer], fbits[kPer], sum = 0;
 #pragma unroll
         for (int j = 0; j < kPer; ++j) {
@@ -309,7 +332,7 @@ __device__ bool bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int
             base += fcount[j];
         }
     }
-    __syncthreads();
+    row_sync<W>();
     // 3. fine histogram
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i) {
@@ -321,7 +344,7 @@ __device__ bool bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int
             bump16(fc, f[i]);
         }
     }
-    __syncthreads();
+    row_sync<W>();
     // 4. exclusive scan of the fine counters (at most P of them; contiguous
     //    words per thread), and the largest fine bucket
     {
@@ -345,7 +368,7 @@ __device__ bool bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int
             base += lo + (x >> 16);
         }
     }
-    __syncthreads();
+    row_sync<W>();
     // 5. scatter into the fine buckets (any order inside a bucket)
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i) {
@@ -354,13 +377,14 @@ __device__ bool bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int
             const uint32_t at = bump16(fc, f[i]);
             if constexpr (PACKED) {
                 sm.keys[at] = (k[i] << kSeqBits) | static_cast<uint32_t>(pos);
+                if constexpr (kStoreFine) sm.seqs[at] = static_cast<uint16_t>(f[i]);
             } else {
                 sm.keys[at] = k[i] + cmin;  // the unpacked layout keeps columns
                 sm.seqs[at] = static_cast<uint16_t>(pos);
             }
         }
     }
-    __syncthreads();
+    row_sync<W>();
     // 6. every sorted position takes its product's place inside the product's
     //    bucket: the number of the bucket's products with a smaller (column,
     //    sequence) pair.  Positions run in lane order, so the lanes of a warp
@@ -376,9 +400,14 @@ __device__ bool bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int
         dst[i] = 0u;
         if (p < P) {
             key[i] = sm.keys[p];
-            const uint32_t kk = PACKED ? key[i] >> kSeqBits : key[i] - cmin;
-            const uint32_t in = info[kk >> sc];
-            const uint32_t fb = (in & 0xffffu) + ((kk & scmask) >> (sc - static_cast<int>(in >> 16)));
+            uint32_t fb;
+            if constexpr (PACKED && kStoreFine) {
+                fb = sm.seqs[p];
+            } else {
+                const uint32_t kk = PACKED ? key[i] >> kSeqBits : key[i] - cmin;
+                const uint32_t in = info[kk >> sc];
+                fb = (in & 0xffffu) + ((kk & scmask) >> (sc - static_cast<int>(in >> 16)));
+            }
             const uint32_t end = half16(fc, fb);
             const uint32_t beg = fb ? half16(fc, fb - 1u) : 0u;
             uint32_t r = 0;
@@ -395,7 +424,7 @@ __device__ bool bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int
             dst[i] = beg + r;
         }
     }
-    __syncthreads();
+    row_sync<W>();
     // 7. products at their sorted positions
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i) {
@@ -405,7 +434,7 @@ __device__ bool bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int
             if constexpr (!PACKED) sm.seqs[dst[i]] = static_cast<uint16_t>(sqv[i]);
         }
     }
-    __syncthreads();
+    row_sync<W>();
     return true;
 }
 
@@ -547,10 +576,14 @@ __device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double*
                            int nbits, int lane, int warp, int tid) {
     using Sm = RowSmem<W, ITEMS, SV>;
     constexpr int kSeqBits = Sm::kSeqBits;
-    // 2. sort by column: the bucket sort for CTA rows, the radix sort for warp
-    //    rows and where the bucket sort declines
-    if constexpr (W == 1) {
+    // 2. sort by column: the bucket sort, or the radix sort for the smallest
+    //    warp rows, for the 512-product warp rows and where the bucket sort
+    //    declines
+    if constexpr (!kBucketRows<W, ITEMS>) {
         radix_sort_row<W, ITEMS, SV, PACKED, true>(sm, P, cmin, nbits, lane, warp, tid);
+    } else if constexpr (W == 1) {
+        if (nbits == 0 || !bucket_sort<W, ITEMS, SV, PACKED>(sm, P, cmin, nbits, lane, warp, tid))
+            radix_sort_row<W, ITEMS, SV, PACKED, true>(sm, P, cmin, nbits, lane, warp, tid);
     } else {
         if (nbits == 0 || !bucket_sort<W, ITEMS, SV, PACKED>(sm, P, cmin, nbits, lane, warp, tid))
             radix_sort_fallback<W, ITEMS, SV, PACKED>(sm, P, cmin, nbits, lane, warp, tid);
