@@ -394,11 +394,16 @@ def batched_subset_record(local: int, count: int = BATCH_SUBSET) -> dict:
                 r.free()
             return eng.last_timings()["launches"]
 
+        device_ms = []
+
         def one_by_one():
             launches = 0
+            device_ms.clear()
             for a, b in dev:
                 eng.multiply(a, b, out="device").free()
-                launches += eng.last_timings()["launches"]
+                t = eng.last_timings()
+                launches += t["launches"]
+                device_ms.append(t["ms_total"])
             return launches
 
         for _ in range(2):
@@ -408,6 +413,7 @@ def batched_subset_record(local: int, count: int = BATCH_SUBSET) -> dict:
         tb = sum(_wall(batched)[0] for _ in range(reps)) / reps
         ts = sum(_wall(one_by_one)[0] for _ in range(reps)) / reps
         lb, ls = batched(), one_by_one()
+        kernels_ms = sum(device_ms)  # first to last event of each call, summed
     return {"workload": WORKLOADS["batched"] + f" [first {count} of {BATCH_PRODUCTS} products]",
             "products": count, "rows_total": int(sum(a.rows for a, _ in pairs)),
             "scalar_products_per_step": int(products), "steps": reps,
@@ -415,7 +421,10 @@ def batched_subset_record(local: int, count: int = BATCH_SUBSET) -> dict:
             "batched": {"value": 2.0 * products / tb / 1e9, "unit": "GFLOP/s", "ms_per_step": 1e3 * tb,
                         "gpu_launches_per_step": int(lb), "what": "one spg_multiply_batch call"},
             "per_product": {"value": 2.0 * products / ts / 1e9, "unit": "GFLOP/s", "ms_per_step": 1e3 * ts,
-                            "gpu_launches_per_step": int(ls), "what": "one spg_multiply call per product"},
+                            "gpu_launches_per_step": int(ls), "what": "one spg_multiply call per product",
+                            "device_ms_per_step": kernels_ms,
+                            "host_overhead_ms_per_step": 1e3 * ts - kernels_ms,
+                            "ceiling_over_per_product": 1e3 * ts / kernels_ms if kernels_ms > 0 else None},
             "batched_over_per_product": ts / tb}
 
 

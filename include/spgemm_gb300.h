@@ -166,8 +166,11 @@ spg_status spg_last_timings(const spg_handle* handle, spg_timings* timings);
 
 /* ---- bin autotuner ----------------------------------------------------------------
  * No reference counterpart.  Several numeric bins have two team shapes (warps
- * per CTA x products per thread); results are identical, times differ with the
- * workload.  spg_tune multiplies A * B reps times (after one warm-up) with every
+ * per CTA x products per thread); for bins 17 and 18 (8,193-16,384 scalar
+ * products per row) the two choices are the threshold above which rows are
+ * split into column-range pieces: at 8,192 (default) or at 16,384, the rows in
+ * between then running whole, one 16-warp CTA each.  Results are identical,
+ * times differ with the workload.  spg_tune multiplies A * B reps times (after one warm-up) with every
  * bin on its default shape, then on its alternative, and keeps, per bin, the
  * alternative where its median numeric time was at least 3% lower.  The choice
  * stays on the handle for later multiplies, batches, to-host products and plans

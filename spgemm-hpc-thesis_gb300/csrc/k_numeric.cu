@@ -482,6 +482,11 @@ size_t numeric_scratch_bytes(const int64_t* bin_count, int64_t max_ub, const Spl
     size_t need = 0;
     if (holes) {
         if (split.rows > 0) need = split_layout(max_ub, split, num_sms).bytes;
+        // bins 17 and 18 run whole where the autotuner chose it (same region:
+        // these launches run one after the other on one stream)
+        for (int b = kLastSmemBin + 1; b < kBinHeavy; ++b)
+            if (bin_count[b])
+                need = std::max(need, static_cast<size_t>(slab_grid(bin_count[b], num_sms)) * slab_cap(b) * sizeof(double));
     } else {
         for (int b = kLastSmemBin + 1; b < kBinHeavy; ++b)  // the launches run one after the other
             if (bin_count[b])
@@ -535,7 +540,12 @@ void launch_numeric(int bin, const Job* d_jobs, const int64_t* d_items, int64_t 
         launch_numeric_warp(bin, d_jobs, d_items, count, d_stats, d_err, st, num_sms);
         return;
     }
-    if (holes && bin > kLastSmemBin) {
+    // Rows above 8,192 products are split into column-range pieces in the
+    // upper-bound layout; the alternative of bins 17 and 18 (8,193-16,384
+    // products) runs those rows whole, one 16-warp CTA each, as the exact layout
+    // does -- the autotuner keeps it where it measures faster.
+    const bool whole = variant == 1 && bin < kBinHeavy;
+    if (holes && bin > kLastSmemBin && !whole) {
         launch_split(d_jobs, d_items, count, max_ub, split, d_scratch, d_stats, d_err, st, num_sms);
         return;
     }

@@ -3,6 +3,8 @@
 // (k_numeric_row.cuh), so results are identical; only the time differs.
 //   bins 7-8   (<= 384, <= 512 products): a 2-warp CTA per row instead of one warp
 //   bins 9-15  (<= 768 ... <= 6144):      the shapes before the last measurement-driven tuning
+//   bins 17-18 (<= 12288, <= 16384):      whole rows, one 16-warp CTA each, instead of
+//                                         column-range pieces (upper-bound layout; k_numeric.cu)
 #include "k_numeric_row.cuh"
 
 namespace spg {

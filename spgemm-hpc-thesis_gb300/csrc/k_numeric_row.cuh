@@ -55,31 +55,42 @@ __device__ __forceinline__ int hidx(int d, int w) {
     return W == 1 ? d : d * kHistStride<W> + w;
 }
 
-// Bucket sort (bucket_sort below): 2^kCoarseBits<W> coarse buckets, whose
-// 16-bit counters take kBkCoarseWords<W> words and whose table (first fine
-// bucket, fine bits) kBkInfoWords<W>; then at most one fine counter per
-// product.  Warp rows take 32 coarse buckets, so that the counters fit the
-// space of their radix counters.
+// Bucket sort of CTA rows (bucket_sort below): 2^kCoarseBits<W> coarse
+// buckets, whose 16-bit counters take kBkCoarseWords<W> words and whose table
+// (first fine bucket, fine bits) kBkInfoWords<W>; then at most one fine
+// counter per product.  (7 coarse bits measured 0.25 ms slower on the
+// power-law product.)
 template <int W>
-constexpr int kCoarseBits = W == 1 ? 5 : 8;
+constexpr int kCoarseBits = 8;
 template <int W>
 constexpr int kBkCoarseWords = (1 << kCoarseBits<W>) / 2;
 template <int W>
 constexpr int kBkInfoWords = 1 << kCoarseBits<W>;
 template <int W, int ITEMS>
 constexpr int kBkWords = kBkCoarseWords<W> + kBkInfoWords<W> + W * 32 * ITEMS / 2 + 1;
-// Warp rows of at least this many products per lane take the bucket sort
-// where its counters fit (up to 12 per lane); smaller ones the radix sort.
-constexpr int kWarpBucketItems = 3;
+
 // In the packed layout the scatter also stores every product's fine bucket
 // beside it (in the sequence-number array, which that layout leaves unused),
-// so that ranking a position reads its bucket instead of recomputing it.
+// so that ranking a position reads its bucket instead of recomputing it from
+// the coarse table (0.29 ms of K4 on the power-law product).
 constexpr bool kStoreFine = true;
+// Upper-bound layout: the bucket sort writes the row's slots itself (see
+// bucket_sort), instead of a separate output pass over the sorted products.
+constexpr bool kFuseOutput = true;
+// Which rows take the bucket sort: CTA rows.  Warp rows keep the radix sort,
+// whose passes need no barrier across warps; the bucket sort for warp rows of
+// 3-12 products per lane (32 coarse buckets) measured 0.1 ms slower on the
+// power-law product and 2% slower on the uniform one.
 template <int W, int ITEMS>
-constexpr bool kBucketRows = W > 1 || (ITEMS >= kWarpBucketItems && kBkWords<1, ITEMS> <= kHistWords<1>);
+constexpr bool kBucketRows = W > 1;
 // A fine bucket holding more products than this (a column repeated many times)
 // sends the row to the radix sort: ranking inside a bucket is quadratic.
 constexpr uint32_t kMaxFine = 64;
+
+// Digit-counter sets of CTA rows.  CTA rows take the radix sort only where the
+// bucket sort declines, so one set (an extra barrier per pass) leaves them more
+// shared memory.
+constexpr int kHistSets = 1;
 
 // SV: product values in shared memory (else in a per-CTA global slab).
 template <int W, int ITEMS, bool SV = true>
@@ -91,10 +102,10 @@ struct RowSmem {
     int64_t warp_tmp[W + 1];    // block scans
     uint32_t keys[kCap];        // columns (unpacked) or packed (column, sequence) words
     union {
-        // digit counters of the radix sort at hidx<W>(digit, warp); CTA rows
-        // alternate two sets so that clearing the next pass's set needs no
-        // barrier of its own
-        alignas(16) uint32_t hist[W == 1 ? 1 : 2][kHistWords<W>];
+        // digit counters of the radix sort at hidx<W>(digit, warp); with two
+        // sets (kHistSets) CTA rows alternate them so that clearing the next
+        // pass's set needs no barrier of its own
+        alignas(16) uint32_t hist[W == 1 ? 1 : kHistSets][kHistWords<W>];
         // bucket sort of CTA rows: coarse counters, coarse bucket table, fine
         // counters (16-bit counters, two per word)
         alignas(16) uint32_t bk[kBucketRows<W, ITEMS> ? kBkWords<W, ITEMS> : 1];
@@ -208,6 +219,17 @@ __device__ inline void scan_kept(uint32_t* cnt, int32_t* red, int warp, int lane
     }
 }
 
+// Where a row's result goes, read once from the Job (locals, not reloaded
+// through the Job reference after every global store).
+struct RowOut {
+    int32_t* __restrict__ c_col;
+    double* __restrict__ c_val;
+    int64_t out0;       // first slot of the row in C_tmp
+    int64_t* nz;        // the row's stored-entry count
+    int32_t holes;      // upper-bound mode: slot-per-position output with holes
+    int32_t nz_add;     // a piece of a split row: add to *nz instead of storing it
+};
+
 // 16-bit counter i of an array of packed pairs (low half: even i).
 __device__ __forceinline__ uint32_t half16(const uint32_t* a, uint32_t i) {
     return (a[i >> 1] >> ((i & 1u) << 4)) & 0xffffu;
@@ -284,14 +306,22 @@ __device__ inline uint32_t block_excl_scan_max(uint32_t v, uint32_t m, int32_t* 
 // takes the radix sort.  On success keys (and seqs when !PACKED) hold the sorted
 // products in the layout finish_row reads: packed (column - cmin, sequence)
 // words, or columns and 16-bit sequence numbers side by side.
+//
+// With `fused` (the upper-bound layout), the output is written here too: a
+// product whose column no other product of its bucket shares -- most of them,
+// since scalar products outnumber stored entries by only a few percent on
+// typical rows -- writes its slot (column, value; a hole for an exact zero) as
+// it moves to its place, non-first products of a repeated column write holes,
+// and the first product of every repeated column sums the column's run in
+// sequence order once all are placed.  Returns 0 when declined, 1 when sorted,
+// 2 when sorted and written (the row's stored count included).
 template <int W, int ITEMS, bool SV, bool PACKED>
-__device__ bool bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int nbits, int lane, int warp,
-                            int tid) {
+__device__ int bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int nbits, int lane, int warp, int tid,
+                           const RowOut* fused = nullptr, const double* vals = nullptr) {
     using Sm = RowSmem<W, ITEMS, SV>;
     constexpr int NT = W * 32;
     constexpr int kSeqBits = Sm::kSeqBits;
     static_assert(kBucketRows<W, ITEMS>, "rows of this shape have no bucket counters");
-    static_assert(sizeof(sm.bk) <= sizeof(sm.hist), "bucket counters share the radix counters' space");
     uint32_t* cc = sm.bk;                                     // coarse counters
     uint32_t* info = sm.bk + kBkCoarseWords<W>;                  // first fine bucket | fine bits << 16
     uint32_t* fc = sm.bk + kBkCoarseWords<W> + kBkInfoWords<W>;     // fine counters, then starts, then ends
@@ -315,7 +345,7 @@ __device__ bool bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int
     // 2. fine buckets of every coarse bucket, numbered in coarse order (one
     //    warp)
     if (warp == 0) {
-        constexpr int kPer = (1 << kCoarseBits<W>) / 32;  // 8 for CTA rows, 1 for warp rows
+        constexpr int kPer = (1 << kCoarseBits<W>) / 32;  // coarse buckets per lane
         uint32_t fcount[kPer], fbits[kPer], sum = 0;
 #pragma unroll
         for (int j = 0; j < kPer; ++j) {
@@ -360,7 +390,7 @@ __device__ bool bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int
         }
         uint32_t total, gmax;
         uint32_t base = block_excl_scan_max<W>(sum, mx, sm.red, lane, warp, total, gmax);
-        if (gmax > kMaxFine) return false;  // uniform: every thread saw the same maximum
+        if (gmax > kMaxFine) return 0;  // uniform: every thread saw the same maximum
         for (int w = w0; w < w1; ++w) {
             const uint32_t x = fc[w];
             const uint32_t lo = x & 0xffffu;
@@ -410,44 +440,98 @@ __device__ bool bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int
             }
             const uint32_t end = half16(fc, fb);
             const uint32_t beg = fb ? half16(fc, fb - 1u) : 0u;
-            uint32_t r = 0;
+            uint32_t r = 0, same = 0, same_before = 0;  // same: the bucket's products of this column
             if constexpr (PACKED) {
-                for (uint32_t q = beg; q < end; ++q) r += sm.keys[q] < key[i] ? 1u : 0u;
+                for (uint32_t q = beg; q < end; ++q) {
+                    const uint32_t kq = sm.keys[q];
+                    const uint32_t lt = kq < key[i] ? 1u : 0u;
+                    const uint32_t eq = (kq ^ key[i]) < (1u << kSeqBits) ? 1u : 0u;
+                    r += lt;
+                    same += eq;
+                    same_before += eq & lt;
+                }
             } else {
                 const uint32_t sq = sm.seqs[p];
                 for (uint32_t q = beg; q < end; ++q) {
                     const uint32_t kq = sm.keys[q];
-                    r += (kq < key[i] || (kq == key[i] && sm.seqs[q] < sq)) ? 1u : 0u;
+                    const uint32_t eq = kq == key[i] ? 1u : 0u;
+                    const uint32_t lt = (kq < key[i] || (eq && sm.seqs[q] < sq)) ? 1u : 0u;
+                    r += lt;
+                    same += eq;
+                    same_before += eq & lt;
                 }
                 sqv[i] = sq;
             }
-            dst[i] = beg + r;
+            // bit 30: the column repeats; bit 31: not its first product
+            dst[i] = (beg + r) | (same > 1 ? (1u << 30) : 0u) | (same_before ? (1u << 31) : 0u);
         }
     }
     row_sync<W>();
-    // 7. products at their sorted positions
+    // 7. products at their sorted positions (and, fused, the slots of columns
+    //    that occur once and the holes of repeated ones)
+    constexpr uint32_t kPosMask = (1u << 30) - 1u;
+    constexpr uint32_t kSeqMask = (1u << kSeqBits) - 1u;
+    uint32_t kept = 0;
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i) {
         const int p = (warp * ITEMS + i) * 32 + lane;
         if (p < P) {
-            sm.keys[dst[i]] = key[i];
-            if constexpr (!PACKED) sm.seqs[dst[i]] = static_cast<uint16_t>(sqv[i]);
+            const uint32_t d = dst[i] & kPosMask;
+            sm.keys[d] = key[i];
+            if constexpr (!PACKED) sm.seqs[d] = static_cast<uint16_t>(sqv[i]);
+            if (fused) {
+                const int64_t slot = fused->out0 + d;
+                if (!(dst[i] & (1u << 30))) {
+                    const uint32_t seq = PACKED ? key[i] & kSeqMask : sqv[i];
+                    const double v = vals[seq];
+                    const int32_t oc = v != 0.0 ? static_cast<int32_t>(PACKED ? (key[i] >> kSeqBits) + cmin : key[i])
+                                                : -1;
+                    fused->c_col[slot] = oc;
+                    if (oc >= 0) {
+                        fused->c_val[slot] = v;
+                        ++kept;
+                    }
+                } else if (dst[i] >> 31) {
+                    fused->c_col[slot] = -1;
+                }
+            }
         }
     }
     row_sync<W>();
-    return true;
+    if (!fused) return 1;
+    // 8. the first product of every repeated column sums the column's run in
+    //    sequence order (the sorted order inside a column)
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+        const int p = (warp * ITEMS + i) * 32 + lane;
+        if (p < P && (dst[i] >> 30) == 1u) {
+            const uint32_t d = dst[i] & kPosMask;
+            const uint32_t c = PACKED ? key[i] >> kSeqBits : key[i];
+            auto col_at = [&](uint32_t q) { return PACKED ? sm.keys[q] >> kSeqBits : sm.keys[q]; };
+            auto seq_at = [&](uint32_t q) { return PACKED ? sm.keys[q] & kSeqMask : static_cast<uint32_t>(sm.seqs[q]); };
+            double acc = vals[seq_at(d)];
+            for (uint32_t q = d + 1; q < static_cast<uint32_t>(P) && col_at(q) == c; ++q)
+                acc = __dadd_rn(acc, vals[seq_at(q)]);
+            const int64_t slot = fused->out0 + d;
+            const int32_t oc = acc != 0.0 ? static_cast<int32_t>(PACKED ? c + cmin : c) : -1;
+            fused->c_col[slot] = oc;
+            if (oc >= 0) {
+                fused->c_val[slot] = acc;
+                ++kept;
+            }
+        }
+    }
+    kept = warp_sum(kept);
+    if (lane == 0) atomicAdd(&sm.kept, kept);
+    __syncthreads();
+    if (tid == 0) {
+        if (fused->nz_add) atomicAdd(reinterpret_cast<unsigned long long*>(fused->nz), static_cast<unsigned long long>(sm.kept));
+        else *fused->nz = sm.kept;
+    }
+    row_sync<W>();
+    return 2;
 }
 
-// Where a row's result goes, read once from the Job (locals, not reloaded
-// through the Job reference after every global store).
-struct RowOut {
-    int32_t* __restrict__ c_col;
-    double* __restrict__ c_val;
-    int64_t out0;       // first slot of the row in C_tmp
-    int64_t* nz;        // the row's stored-entry count
-    int32_t holes;      // upper-bound mode: slot-per-position output with holes
-    int32_t nz_add;     // a piece of a split row: add to *nz instead of storing it
-};
 
 // The stable LSD radix sort of a row's products by column: 8-bit digits over
 // the bits of max(col) - min(col), and with kNarrow a last pass of at most 4
@@ -543,9 +627,12 @@ __device__ __forceinline__ void radix_sort_row(RowSmem<W, ITEMS, SV>& sm, int P,
         if constexpr (W == 1) {
             __syncwarp();
             if (more) clear_counters<W>(sm.hist[0], digits_from(shift), tid);
-        } else {
+        } else if constexpr (kHistSets == 2) {
             if (more) clear_counters<W>(sm.hist[hb ^ 1], digits_from(shift), tid);
             hb ^= 1;
+        } else {
+            __syncthreads();  // the scatter above still reads the counters
+            if (more) clear_counters<W>(sm.hist[0], digits_from(shift), tid);
         }
         row_sync<W>();
     }
@@ -576,17 +663,17 @@ __device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double*
                            int nbits, int lane, int warp, int tid) {
     using Sm = RowSmem<W, ITEMS, SV>;
     constexpr int kSeqBits = Sm::kSeqBits;
-    // 2. sort by column: the bucket sort, or the radix sort for the smallest
-    //    warp rows, for the 512-product warp rows and where the bucket sort
-    //    declines
+    // 2. sort by column: the bucket sort for CTA rows, the radix sort for warp
+    //    rows and where the bucket sort declines
     if constexpr (!kBucketRows<W, ITEMS>) {
         radix_sort_row<W, ITEMS, SV, PACKED, true>(sm, P, cmin, nbits, lane, warp, tid);
-    } else if constexpr (W == 1) {
-        if (nbits == 0 || !bucket_sort<W, ITEMS, SV, PACKED>(sm, P, cmin, nbits, lane, warp, tid))
-            radix_sort_row<W, ITEMS, SV, PACKED, true>(sm, P, cmin, nbits, lane, warp, tid);
     } else {
-        if (nbits == 0 || !bucket_sort<W, ITEMS, SV, PACKED>(sm, P, cmin, nbits, lane, warp, tid))
-            radix_sort_fallback<W, ITEMS, SV, PACKED>(sm, P, cmin, nbits, lane, warp, tid);
+        const int done = nbits == 0 ? 0
+                                    : bucket_sort<W, ITEMS, SV, PACKED>(sm, P, cmin, nbits, lane, warp, tid,
+                                                                        (kFuseOutput && out.holes) ? &out : nullptr,
+                                                                        vals);
+        if (done == 2) return;  // written in the sort's last steps
+        if (done == 0) radix_sort_fallback<W, ITEMS, SV, PACKED>(sm, P, cmin, nbits, lane, warp, tid);
     }
 
     // Column and sequence number of sorted position pos.
@@ -839,7 +926,7 @@ void run_block(const Job* jobs, const int64_t* items, int64_t count, Stats* stat
                int num_sms, double* gvals = nullptr) {
     const int smem = static_cast<int>(sizeof(RowSmem<W, ITEMS, SV>));
     cudaFuncSetAttribute(num_block_kernel<W, ITEMS, MINB, SV>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    const int grid = SV ? capped(count, 1, num_sms * 8) : slab_grid(count, num_sms, MINB);
+    const int grid = SV ? capped(count, 1, num_sms * (MINB > 8 ? MINB : 8)) : slab_grid(count, num_sms, MINB);
     num_block_kernel<W, ITEMS, MINB, SV><<<grid, W * 32, smem, st>>>(jobs, items, count, stats, err, gvals);
 }
 
