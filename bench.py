@@ -428,6 +428,33 @@ def batched_subset_record(local: int, count: int = BATCH_SUBSET) -> dict:
             "batched_over_per_product": ts / tb}
 
 
+def served_subset_record(local: int, requests: int = 200, rate: float = 1000.0) -> dict:
+    """The served stream, bounded: the full request pool, every request queued at
+    once (saturation) and a Poisson trace at one rate, through continuous
+    batching (3 lanes, batches of <= 256 requests / 2^27 scalar products) and
+    through per-request launches (1 lane, batches of 1)."""
+    import spgemm_gb300 as sg
+    pool = make_workload("served")
+    products = [sg.scalar_products_host(a, b) for a, b in pool]
+    dev = [(a.to_device(local), b.to_device(local)) for a, b in pool]
+    modes = {"batched": dict(lanes=3, max_batch=256, max_batch_products=1 << 27),
+             "per_request": dict(lanes=1, max_batch=1)}
+    out = {}
+    for mode, kw in modes.items():
+        with sg.Server(local, hbm_budget_bytes=150 * 10**9, **kw) as srv:
+            _serve_trace(srv, dev, products, np.zeros(len(pool)), np.arange(len(pool)))  # warm-up
+            _, picks = _arrivals(1.0, requests, len(pool), seed=7)
+            sat = _serve_trace(srv, dev, products, np.zeros(requests), picks)
+            at, picks = _arrivals(rate, requests, len(pool), seed=int(rate))
+            paced = _serve_trace(srv, dev, products, at, picks)
+        out[mode] = {"saturation": sat, f"poisson_{int(rate)}_req_per_s": paced}
+    return {"workload": WORKLOADS["served"], "pool": len(pool), "requests_per_trace": requests,
+            "modes": modes, "by_mode": out,
+            "batched_over_per_request": out["batched"]["saturation"]["req_per_s"]
+            / out["per_request"]["saturation"]["req_per_s"],
+            "timing": "server-side submit-to-ready latency; span on the host clock"}
+
+
 def run_gpu_arm(args, rank, world, local):
     import torch
     import spgemm_gb300 as sg
@@ -537,6 +564,7 @@ def run_gpu_arm(args, rank, world, local):
         eng = None
         subs = {name: sub_record(name, min(args.steps, 10), args.warmup, local) for name in ("uniform", "galerkin")}
         subs["batched_subset"] = batched_subset_record(local)
+        subs["served_subset"] = served_subset_record(local)
 
     if rank == 0:
         line = {
@@ -805,7 +833,7 @@ def main():
     ap.add_argument("--no-replay", action="store_true", help="skip the plan-replay (CUDA graph) sub-measurement")
     ap.add_argument("--no-tune", action="store_true", help="keep the default team shape in every bin")
     ap.add_argument("--no-sub", action="store_true",
-                    help="skip the uniform, Galerkin and batched-subset records of the default line")
+                    help="skip the uniform, Galerkin, batched-subset and served-subset records of the default line")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -74,9 +74,6 @@ constexpr int kBkWords = kBkCoarseWords<W> + kBkInfoWords<W> + W * 32 * ITEMS / 
 // so that ranking a position reads its bucket instead of recomputing it from
 // the coarse table (0.29 ms of K4 on the power-law product).
 constexpr bool kStoreFine = true;
-// Upper-bound layout: the bucket sort writes the row's slots itself (see
-// bucket_sort), instead of a separate output pass over the sorted products.
-constexpr bool kFuseOutput = true;
 // Which rows take the bucket sort: CTA rows.  Warp rows keep the radix sort,
 // whose passes need no barrier across warps; the bucket sort for warp rows of
 // 3-12 products per lane (32 coarse buckets) measured 0.1 ms slower on the
@@ -306,18 +303,9 @@ __device__ inline uint32_t block_excl_scan_max(uint32_t v, uint32_t m, int32_t* 
 // takes the radix sort.  On success keys (and seqs when !PACKED) hold the sorted
 // products in the layout finish_row reads: packed (column - cmin, sequence)
 // words, or columns and 16-bit sequence numbers side by side.
-//
-// With `fused` (the upper-bound layout), the output is written here too: a
-// product whose column no other product of its bucket shares -- most of them,
-// since scalar products outnumber stored entries by only a few percent on
-// typical rows -- writes its slot (column, value; a hole for an exact zero) as
-// it moves to its place, non-first products of a repeated column write holes,
-// and the first product of every repeated column sums the column's run in
-// sequence order once all are placed.  Returns 0 when declined, 1 when sorted,
-// 2 when sorted and written (the row's stored count included).
 template <int W, int ITEMS, bool SV, bool PACKED>
-__device__ int bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int nbits, int lane, int warp, int tid,
-                           const RowOut* fused = nullptr, const double* vals = nullptr) {
+__device__ bool bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int nbits, int lane, int warp,
+                            int tid) {
     using Sm = RowSmem<W, ITEMS, SV>;
     constexpr int NT = W * 32;
     constexpr int kSeqBits = Sm::kSeqBits;
@@ -390,7 +378,7 @@ __device__ int bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int 
         }
         uint32_t total, gmax;
         uint32_t base = block_excl_scan_max<W>(sum, mx, sm.red, lane, warp, total, gmax);
-        if (gmax > kMaxFine) return 0;  // uniform: every thread saw the same maximum
+        if (gmax > kMaxFine) return false;  // uniform: every thread saw the same maximum
         for (int w = w0; w < w1; ++w) {
             const uint32_t x = fc[w];
             const uint32_t lo = x & 0xffffu;
@@ -440,96 +428,32 @@ __device__ int bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int 
             }
             const uint32_t end = half16(fc, fb);
             const uint32_t beg = fb ? half16(fc, fb - 1u) : 0u;
-            uint32_t r = 0, same = 0, same_before = 0;  // same: the bucket's products of this column
+            uint32_t r = 0;
             if constexpr (PACKED) {
-                for (uint32_t q = beg; q < end; ++q) {
-                    const uint32_t kq = sm.keys[q];
-                    const uint32_t lt = kq < key[i] ? 1u : 0u;
-                    const uint32_t eq = (kq ^ key[i]) < (1u << kSeqBits) ? 1u : 0u;
-                    r += lt;
-                    same += eq;
-                    same_before += eq & lt;
-                }
+                for (uint32_t q = beg; q < end; ++q) r += sm.keys[q] < key[i] ? 1u : 0u;
             } else {
                 const uint32_t sq = sm.seqs[p];
                 for (uint32_t q = beg; q < end; ++q) {
                     const uint32_t kq = sm.keys[q];
-                    const uint32_t eq = kq == key[i] ? 1u : 0u;
-                    const uint32_t lt = (kq < key[i] || (eq && sm.seqs[q] < sq)) ? 1u : 0u;
-                    r += lt;
-                    same += eq;
-                    same_before += eq & lt;
+                    r += (kq < key[i] || (kq == key[i] && sm.seqs[q] < sq)) ? 1u : 0u;
                 }
                 sqv[i] = sq;
             }
-            // bit 30: the column repeats; bit 31: not its first product
-            dst[i] = (beg + r) | (same > 1 ? (1u << 30) : 0u) | (same_before ? (1u << 31) : 0u);
+            dst[i] = beg + r;
         }
     }
     row_sync<W>();
-    // 7. products at their sorted positions (and, fused, the slots of columns
-    //    that occur once and the holes of repeated ones)
-    constexpr uint32_t kPosMask = (1u << 30) - 1u;
-    constexpr uint32_t kSeqMask = (1u << kSeqBits) - 1u;
-    uint32_t kept = 0;
+    // 7. products at their sorted positions
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i) {
         const int p = (warp * ITEMS + i) * 32 + lane;
         if (p < P) {
-            const uint32_t d = dst[i] & kPosMask;
-            sm.keys[d] = key[i];
-            if constexpr (!PACKED) sm.seqs[d] = static_cast<uint16_t>(sqv[i]);
-            if (fused) {
-                const int64_t slot = fused->out0 + d;
-                if (!(dst[i] & (1u << 30))) {
-                    const uint32_t seq = PACKED ? key[i] & kSeqMask : sqv[i];
-                    const double v = vals[seq];
-                    const int32_t oc = v != 0.0 ? static_cast<int32_t>(PACKED ? (key[i] >> kSeqBits) + cmin : key[i])
-                                                : -1;
-                    fused->c_col[slot] = oc;
-                    if (oc >= 0) {
-                        fused->c_val[slot] = v;
-                        ++kept;
-                    }
-                } else if (dst[i] >> 31) {
-                    fused->c_col[slot] = -1;
-                }
-            }
+            sm.keys[dst[i]] = key[i];
+            if constexpr (!PACKED) sm.seqs[dst[i]] = static_cast<uint16_t>(sqv[i]);
         }
     }
     row_sync<W>();
-    if (!fused) return 1;
-    // 8. the first product of every repeated column sums the column's run in
-    //    sequence order (the sorted order inside a column)
-#pragma unroll
-    for (int i = 0; i < ITEMS; ++i) {
-        const int p = (warp * ITEMS + i) * 32 + lane;
-        if (p < P && (dst[i] >> 30) == 1u) {
-            const uint32_t d = dst[i] & kPosMask;
-            const uint32_t c = PACKED ? key[i] >> kSeqBits : key[i];
-            auto col_at = [&](uint32_t q) { return PACKED ? sm.keys[q] >> kSeqBits : sm.keys[q]; };
-            auto seq_at = [&](uint32_t q) { return PACKED ? sm.keys[q] & kSeqMask : static_cast<uint32_t>(sm.seqs[q]); };
-            double acc = vals[seq_at(d)];
-            for (uint32_t q = d + 1; q < static_cast<uint32_t>(P) && col_at(q) == c; ++q)
-                acc = __dadd_rn(acc, vals[seq_at(q)]);
-            const int64_t slot = fused->out0 + d;
-            const int32_t oc = acc != 0.0 ? static_cast<int32_t>(PACKED ? c + cmin : c) : -1;
-            fused->c_col[slot] = oc;
-            if (oc >= 0) {
-                fused->c_val[slot] = acc;
-                ++kept;
-            }
-        }
-    }
-    kept = warp_sum(kept);
-    if (lane == 0) atomicAdd(&sm.kept, kept);
-    __syncthreads();
-    if (tid == 0) {
-        if (fused->nz_add) atomicAdd(reinterpret_cast<unsigned long long*>(fused->nz), static_cast<unsigned long long>(sm.kept));
-        else *fused->nz = sm.kept;
-    }
-    row_sync<W>();
-    return 2;
+    return true;
 }
 
 
@@ -668,12 +592,8 @@ __device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double*
     if constexpr (!kBucketRows<W, ITEMS>) {
         radix_sort_row<W, ITEMS, SV, PACKED, true>(sm, P, cmin, nbits, lane, warp, tid);
     } else {
-        const int done = nbits == 0 ? 0
-                                    : bucket_sort<W, ITEMS, SV, PACKED>(sm, P, cmin, nbits, lane, warp, tid,
-                                                                        (kFuseOutput && out.holes) ? &out : nullptr,
-                                                                        vals);
-        if (done == 2) return;  // written in the sort's last steps
-        if (done == 0) radix_sort_fallback<W, ITEMS, SV, PACKED>(sm, P, cmin, nbits, lane, warp, tid);
+        if (nbits == 0 || !bucket_sort<W, ITEMS, SV, PACKED>(sm, P, cmin, nbits, lane, warp, tid))
+            radix_sort_fallback<W, ITEMS, SV, PACKED>(sm, P, cmin, nbits, lane, warp, tid);
     }
 
     // Column and sequence number of sorted position pos.
