@@ -74,6 +74,14 @@ constexpr int kBkWords = kBkCoarseWords<W> + kBkInfoWords<W> + W * 32 * ITEMS / 
 // so that ranking a position reads its bucket instead of recomputing it from
 // the coarse table (0.29 ms of K4 on the power-law product).
 constexpr bool kStoreFine = true;
+// Products ranked together in the bucket sort's rank step (see bucket_sort):
+// the largest divisor of ITEMS not above kRankGroup.
+constexpr int kRankGroup = 4;
+constexpr int rank_group(int items) {
+    for (int g = kRankGroup; g > 1; --g)
+        if (items % g == 0) return g;
+    return 1;
+}
 // Which rows take the bucket sort: CTA rows.  Warp rows keep the radix sort,
 // whose passes need no barrier across warps; the bucket sort for warp rows of
 // 3-12 products per lane (32 coarse buckets) measured 0.1 ms slower on the
@@ -411,36 +419,54 @@ __device__ bool bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int
     uint32_t* const dst = f;  // the fine indices are no longer needed
     uint32_t* const key = k;  // nor the column offsets
     uint32_t sqv[PACKED ? 1 : ITEMS];  // sequence numbers of the unpacked layout
+    // Positions are ranked kRankGroup at a time in lock-step: their buckets'
+    // bounds are loaded together, then one loop over the longest of their
+    // buckets issues independent loads for all of them.
+    constexpr int G = rank_group(ITEMS);
 #pragma unroll
-    for (int i = 0; i < ITEMS; ++i) {
-        const int p = (warp * ITEMS + i) * 32 + lane;
-        key[i] = 0u;
-        dst[i] = 0u;
-        if (p < P) {
-            key[i] = sm.keys[p];
-            uint32_t fb;
-            if constexpr (PACKED && kStoreFine) {
-                fb = sm.seqs[p];
-            } else {
-                const uint32_t kk = PACKED ? key[i] >> kSeqBits : key[i] - cmin;
-                const uint32_t in = info[kk >> sc];
-                fb = (in & 0xffffu) + ((kk & scmask) >> (sc - static_cast<int>(in >> 16)));
-            }
-            const uint32_t end = half16(fc, fb);
-            const uint32_t beg = fb ? half16(fc, fb - 1u) : 0u;
-            uint32_t r = 0;
-            if constexpr (PACKED) {
-                for (uint32_t q = beg; q < end; ++q) r += sm.keys[q] < key[i] ? 1u : 0u;
-            } else {
-                const uint32_t sq = sm.seqs[p];
-                for (uint32_t q = beg; q < end; ++q) {
-                    const uint32_t kq = sm.keys[q];
-                    r += (kq < key[i] || (kq == key[i] && sm.seqs[q] < sq)) ? 1u : 0u;
+    for (int i0 = 0; i0 < ITEMS; i0 += G) {
+        uint32_t beg[G], len[G], r[G], maxlen = 0;
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+            const int i = i0 + g;
+            const int p = (warp * ITEMS + i) * 32 + lane;
+            key[i] = 0u;
+            beg[g] = 0u;
+            len[g] = 0u;
+            r[g] = 0u;
+            if (p < P) {
+                key[i] = sm.keys[p];
+                uint32_t fb;
+                if constexpr (PACKED && kStoreFine) {
+                    fb = sm.seqs[p];
+                } else {
+                    const uint32_t kk = PACKED ? key[i] >> kSeqBits : key[i] - cmin;
+                    const uint32_t in = info[kk >> sc];
+                    fb = (in & 0xffffu) + ((kk & scmask) >> (sc - static_cast<int>(in >> 16)));
                 }
-                sqv[i] = sq;
+                if constexpr (!PACKED) sqv[i] = sm.seqs[p];
+                const uint32_t end = half16(fc, fb);
+                beg[g] = fb ? half16(fc, fb - 1u) : 0u;
+                len[g] = end - beg[g];
+                maxlen = max(maxlen, len[g]);
             }
-            dst[i] = beg + r;
         }
+        for (uint32_t q = 0; q < maxlen; ++q) {
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+                const int i = i0 + g;
+                if (q < len[g]) {
+                    const uint32_t kq = sm.keys[beg[g] + q];
+                    if constexpr (PACKED) {
+                        r[g] += kq < key[i] ? 1u : 0u;
+                    } else {
+                        r[g] += (kq < key[i] || (kq == key[i] && sm.seqs[beg[g] + q] < sqv[i])) ? 1u : 0u;
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int g = 0; g < G; ++g) dst[i0 + g] = beg[g] + r[g];
     }
     row_sync<W>();
     // 7. products at their sorted positions
