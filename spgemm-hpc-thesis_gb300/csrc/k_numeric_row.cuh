@@ -75,8 +75,10 @@ constexpr int kBkWords = kBkCoarseWords<W> + kBkInfoWords<W> + W * 32 * ITEMS / 
 // the coarse table (0.29 ms of K4 on the power-law product).
 constexpr bool kStoreFine = true;
 // Products ranked together in the bucket sort's rank step (see bucket_sort):
-// the largest divisor of ITEMS not above kRankGroup.
-constexpr int kRankGroup = 4;
+// the largest divisor of ITEMS not above kRankGroup.  On the power-law product:
+// one at a time 13.96 ms of K4, two 13.75, four 13.91, six 13.87 (register
+// pressure grows with the group).
+constexpr int kRankGroup = 2;
 constexpr int rank_group(int items) {
     for (int g = kRankGroup; g > 1; --g)
         if (items % g == 0) return g;
