@@ -35,7 +35,9 @@ typedef enum {
     SPG_OUT_OF_RANGE_COLUMN = 3,   /* an A column outside B's rows (std::runtime_error in the reference) */
     SPG_OUT_OF_MEMORY = 4,         /* device allocation failed */
     SPG_BUDGET_EXCEEDED = 5,       /* the request's footprint exceeds the handle's HBM budget */
-    SPG_DEVICE_TIMEOUT = 6,        /* a bounded wait ran out (serving loop) */
+    SPG_DEVICE_TIMEOUT = 6,        /* reserved: no call of this library returns it -- no kernel waits on
+                                      another CTA, a flag or a device; an unfinished request polls
+                                      as SPG_NOT_READY */
     SPG_CUDA_ERROR = 7,            /* any other CUDA failure */
     SPG_NOT_READY = 8,             /* spg_poll: the request has not finished */
     SPG_CANCELLED = 9,             /* spg_poll: the request was cancelled */
