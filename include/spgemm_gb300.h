@@ -132,7 +132,10 @@ spg_status spg_multiply(spg_handle* handle, const spg_csr_view* A, const spg_csr
  * later blocks compute, so the transfer of C overlaps the computation.  Page-locked buffers (spg_host_alloc) are needed for the
  * overlap; pageable ones work but copy synchronously.  *c_nnz receives nnz(C);
  * if it exceeds c_capacity the call fails with SPG_BUDGET_EXCEEDED and *c_nnz
- * holds a lower bound of the entries needed.  Results are those of
+ * holds a lower bound of the entries needed.  On any failure (that one, an
+ * input error found in a later row block, a CUDA error) the call returns only
+ * after the copies of earlier blocks have finished, so the caller may reuse or
+ * free its arrays at once.  Results are those of
  * spg_multiply.  Same reference counterpart as spg_multiply: the by-value
  * CsrMatrix return of spgemm() (spgemm_exchange.hpp:37-39). */
 spg_status spg_multiply_to_host(spg_handle* handle, const spg_csr_view* A, const spg_csr_view* B, int64_t* c_row_ptr,
