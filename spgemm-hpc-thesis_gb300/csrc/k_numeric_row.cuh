@@ -105,7 +105,7 @@ struct RowSmem {
     static constexpr int kCap = W * 32 * ITEMS;
     static constexpr int kSeqBits = log2_ceil_c(kCap);
     double vals[SV ? kCap : 1];  // product values by sequence number; run sums in place
-    SegTab<W * 32, int32_t> seg;  // enumeration batch
+    RowSegs<W * 32, W * 32 * ITEMS> seg;  // enumeration batch
     int64_t warp_tmp[W + 1];    // block scans
     uint32_t keys[kCap];        // columns (unpacked) or packed (column, sequence) words
     union {
@@ -768,10 +768,10 @@ __device__ void numeric_row(const Job& J, int row, RowSmem<W, ITEMS, SV>& sm, do
         staged_products_in<W * 32>(pc->scol, pc->sval, static_cast<int32_t>(J.ub[row]), sm.step_cnt, tid, pc->lo,
                                    pc->hi, put);
     else
-        team_products<W * 32, true, int32_t>(J, row, sm.seg, sm.warp_tmp, tid,
-                                             [&](int32_t seq, int32_t c, double b, double a) {
-                                                 put(seq, c, __dmul_rn(a, b));
-                                             });
+        team_row_products<W * 32, Sm::kCap>(J, row, sm.seg, sm.warp_tmp, tid,
+                                            [&](int32_t seq, int32_t c, double b, double a) {
+                                                put(seq, c, __dmul_rn(a, b));
+                                            });
     lo = warp_min(lo);
     hi = warp_max(hi);
     if (W > 1) {

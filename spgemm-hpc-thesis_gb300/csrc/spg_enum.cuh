@@ -156,6 +156,96 @@ __device__ inline void team_products(const Job& J, int row, SegTab<NT, Idx>& tab
     }
 }
 
+// Segment table of team_row_products: rows of at most CAP products, NT
+// segments per batch.  Entry r describes the r-th non-empty segment of the
+// batch: the byte addresses of its B columns and values less 4 and 8 bytes
+// times its first position in the batch (so product t of the batch lies at
+// colb[r] + 4t, valb[r] + 8t), and its scale.  word[w] covers batch positions
+// [32w, 32w + 32): x has bit b set where a non-empty segment starts at 32w + b,
+// y is the rank r of the segment holding position 32w.
+template <int NT, int CAP>
+struct RowSegs {
+    static_assert(CAP % 32 == 0 && CAP < 65536, "positions and non-empty counts share one 32-bit scan");
+    uint64_t colb[NT];
+    uint64_t valb[NT];
+    double scale[NT];
+    uint2 word[CAP / 32];
+    int32_t total;
+};
+
+// team_products for rows of at most CAP products (every row the shared-memory
+// row kernels take): the same products, sequence numbers and calls of f, but a
+// product finds its segment from the batch's start mask (one broadcast load and
+// a population count: the rank of the segment holding the word's first
+// position plus the starts between that position and the product's) instead of
+// a binary search over the batch's prefix sums.  t & 31 is the lane for every
+// product a thread takes (the team strides by multiples of 32), so the mask bits
+// at or below the product's position are lanemask_le.
+template <int NT, int CAP, int U = 4, typename F>
+__device__ inline void team_row_products(const Job& J, int row, RowSegs<NT, CAP>& tab, int64_t* s_warp, int tid,
+                                         F&& f) {
+    const bool has_s = J.S.rp != nullptr;
+    const int64_t a0 = J.A.rp[row];
+    const int64_t nseg = (J.A.rp[row + 1] - a0) + (has_s ? 1 : 0);
+    const int lane = tid & 31;
+    const unsigned le_above0 = (lanemask_lt() | (1u << lane)) & ~1u;  // bits (0, lane]
+    int32_t seq_base = 0;
+    for (int64_t e0 = 0; e0 < nseg; e0 += NT) {
+        const int64_t e = e0 + tid;
+        const int32_t* cp = nullptr;
+        const double* vp = nullptr;
+        double sc = 1.0;
+        int32_t len = 0;
+        if (e < nseg) row_segment(J, row, a0, has_s, e, cp, vp, sc, len);
+        // the start mask is cleared before the scan's barriers and set after them
+        for (int w = tid; w < CAP / 32; w += NT) tab.word[w].x = 0u;
+        if constexpr (NT == 32) __syncwarp();
+        // low 16 bits: products; high 16 bits: non-empty segments
+        const uint32_t packed = static_cast<uint32_t>(len) | (len > 0 ? 0x10000u : 0u);
+        uint32_t incl;
+        if constexpr (NT == 32) incl = warp_incl_scan(packed, tid);
+        else incl = block_incl_scan<NT>(packed, s_warp);
+        if (len > 0) {
+            const uint32_t s = (incl & 0xffffu) - static_cast<uint32_t>(len);
+            const uint32_t r = (incl >> 16) - 1u;
+            tab.colb[r] = reinterpret_cast<uint64_t>(cp) - 4u * static_cast<uint64_t>(s);
+            tab.valb[r] = reinterpret_cast<uint64_t>(vp) - 8u * static_cast<uint64_t>(s);
+            tab.scale[r] = sc;
+            atomicOr(&tab.word[s >> 5].x, 1u << (s & 31u));
+            for (uint32_t w = (s + 31u) >> 5; (w << 5) < s + static_cast<uint32_t>(len); ++w) tab.word[w].y = r;
+        }
+        if (tid == NT - 1) tab.total = static_cast<int32_t>(incl & 0xffffu);
+        team_sync<NT>();
+        const int32_t total = tab.total;
+        for (int32_t t0 = tid; t0 < total; t0 += U * NT) {
+            int r[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int32_t t = t0 + u * NT;
+                r[u] = 0;
+                if (t < total) {
+                    const uint2 wd = tab.word[t >> 5];
+                    r[u] = static_cast<int>(wd.y) + __popc(wd.x & le_above0);
+                }
+            }
+            int32_t c[U];
+            double b[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int32_t t = t0 + u * NT;
+                const bool ok = t < total;
+                c[u] = ok ? __ldg(reinterpret_cast<const int32_t*>(tab.colb[r[u]] + 4u * static_cast<uint64_t>(t))) : 0;
+                b[u] = ok ? __ldg(reinterpret_cast<const double*>(tab.valb[r[u]] + 8u * static_cast<uint64_t>(t))) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (t0 + u * NT < total) f(seq_base + t0 + u * NT, c[u], b[u], tab.scale[r[u]]);
+        }
+        seq_base += total;
+        team_sync<NT>();
+    }
+}
+
 // The products of a staged row (columns scol[0..n), values sval[0..n), in the
 // row's product order) whose column lies in [lo, hi), for a whole CTA (NT
 // threads, 8 * NT/32 <= 64).  Kept products are numbered 0, 1, ... in row
