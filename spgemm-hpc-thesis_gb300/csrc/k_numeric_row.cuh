@@ -66,14 +66,30 @@ template <int W>
 constexpr int kBkCoarseWords = (1 << kCoarseBits<W>) / 2;
 template <int W>
 constexpr int kBkInfoWords = 1 << kCoarseBits<W>;
+// Fine bits of a coarse bucket of n products: floor(log2 n) + fine_extra(cap)
+// (at most the bucket's column bits), so P products take at most
+// P << fine_extra(cap) fine counters, plus one past the last; fine bucket
+// numbers stay below 2^16 (they are stored in 16-bit words).  On the power-law
+// product one extra bit measured 1.1% faster than none (buckets of 0.5-1
+// products on average instead of 1-2: shorter rank loops), two 5% slower.
+constexpr int kFineExtraBits = 1;
+constexpr int fine_extra(int cap) {
+    int e = kFineExtraBits;
+    while (e > 0 && (cap << e) >= 65536) --e;
+    return e;
+}
 template <int W, int ITEMS>
-constexpr int kBkWords = kBkCoarseWords<W> + kBkInfoWords<W> + W * 32 * ITEMS / 2 + 1;
+constexpr int kBkWords = kBkCoarseWords<W> + kBkInfoWords<W> + ((W * 32 * ITEMS) << fine_extra(W * 32 * ITEMS)) / 2 + 1;
 
 // In the packed layout the scatter also stores every product's fine bucket
 // beside it (in the sequence-number array, which that layout leaves unused),
 // so that ranking a position reads its bucket instead of recomputing it from
 // the coarse table (0.29 ms of K4 on the power-law product).
 constexpr bool kStoreFine = true;
+// The fine histogram keeps every product's arrival index in its bucket (the
+// counter's old value), so the scatter places products at bucket start plus
+// arrival with no second round of atomics.
+constexpr bool kArrivalScatter = true;
 // Products ranked together in the bucket sort's rank step (see bucket_sort):
 // the largest divisor of ITEMS not above kRankGroup.  On the power-law product:
 // one at a time 13.96 ms of K4, two 13.75, four 13.91, six 13.87 (register
@@ -327,7 +343,9 @@ __device__ bool bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int
     const int sc = nbits - cbits;                             // column bits inside a coarse bucket
     const uint32_t scmask = (1u << sc) - 1u;
     // 0. clear the coarse counters and enough fine counters for P products
-    const int fwords = (P + 1) >> 1;
+    constexpr int kExtra = fine_extra(Sm::kCap);
+    static_assert((Sm::kCap << kExtra) < 65536, "fine bucket numbers are 16-bit");
+    const int fwords = ((P << kExtra) + 2) >> 1;  // one counter past the last fine bucket
     for (int i = tid; i < kBkCoarseWords<W>; i += NT) cc[i] = 0u;
     for (int i = tid; i < fwords; i += NT) fc[i] = 0u;
     row_sync<W>();
@@ -348,7 +366,7 @@ __device__ bool bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int
 #pragma unroll
         for (int j = 0; j < kPer; ++j) {
             const uint32_t n = half16(cc, static_cast<uint32_t>(lane * kPer + j));  // zero beyond 2^cbits
-            const int lg = n ? 31 - __clz(n) : 0;
+            const int lg = n ? 31 - __clz(n) + kExtra : 0;
             fbits[j] = static_cast<uint32_t>(lg < sc ? lg : sc);
             fcount[j] = n ? (1u << fbits[j]) : 0u;
             sum += fcount[j];
@@ -369,7 +387,8 @@ __device__ bool bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int
         if (pos < P) {
             const uint32_t in = info[k[i] >> sc];
             f[i] = (in & 0xffffu) + ((k[i] & scmask) >> (sc - static_cast<int>(in >> 16)));
-            bump16(fc, f[i]);
+            if constexpr (kArrivalScatter) f[i] |= bump16(fc, f[i]) << 16;  // arrival in the high half
+            else bump16(fc, f[i]);
         }
     }
     row_sync<W>();
@@ -402,10 +421,11 @@ __device__ bool bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int
     for (int i = 0; i < ITEMS; ++i) {
         const int pos = (warp * ITEMS + i) * 32 + lane;
         if (pos < P) {
-            const uint32_t at = bump16(fc, f[i]);
+            const uint32_t fi = f[i] & 0xffffu;
+            const uint32_t at = kArrivalScatter ? half16(fc, fi) + (f[i] >> 16) : bump16(fc, fi);
             if constexpr (PACKED) {
                 sm.keys[at] = (k[i] << kSeqBits) | static_cast<uint32_t>(pos);
-                if constexpr (kStoreFine) sm.seqs[at] = static_cast<uint16_t>(f[i]);
+                if constexpr (kStoreFine) sm.seqs[at] = static_cast<uint16_t>(fi);
             } else {
                 sm.keys[at] = k[i] + cmin;  // the unpacked layout keeps columns
                 sm.seqs[at] = static_cast<uint16_t>(pos);
@@ -417,7 +437,8 @@ __device__ bool bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int
     //    bucket: the number of the bucket's products with a smaller (column,
     //    sequence) pair.  Positions run in lane order, so the lanes of a warp
     //    mostly share buckets (same loop bounds, broadcast loads).  The counters
-    //    now hold every bucket's end.
+    //    hold every bucket's start (arrival scatter; the one past the last bucket
+    //    holds P) or its end.
     uint32_t* const dst = f;  // the fine indices are no longer needed
     uint32_t* const key = k;  // nor the column offsets
     uint32_t sqv[PACKED ? 1 : ITEMS];  // sequence numbers of the unpacked layout
@@ -447,8 +468,9 @@ __device__ bool bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int
                     fb = (in & 0xffffu) + ((kk & scmask) >> (sc - static_cast<int>(in >> 16)));
                 }
                 if constexpr (!PACKED) sqv[i] = sm.seqs[p];
-                const uint32_t end = half16(fc, fb);
-                beg[g] = fb ? half16(fc, fb - 1u) : 0u;
+                // counters hold bucket starts (arrival scatter) or ends
+                const uint32_t end = kArrivalScatter ? half16(fc, fb + 1u) : half16(fc, fb);
+                beg[g] = kArrivalScatter ? half16(fc, fb) : (fb ? half16(fc, fb - 1u) : 0u);
                 len[g] = end - beg[g];
                 maxlen = max(maxlen, len[g]);
             }
