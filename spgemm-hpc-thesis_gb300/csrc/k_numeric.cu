@@ -380,10 +380,9 @@ num_piece_kernel(const Job* __restrict__ jobs, SplitPlan plan, Stats* __restrict
         const Piece pc = plan.pieces[i];
         if (pc.count <= 0) continue;  // an empty last piece (same for the whole CTA)
         const Job& J = jobs[item_job(pc.item)];
-        numeric_row<W, ITEMS, false, true>(J, item_row(pc.item), sm, vals, err, &pc);
-        if (threadIdx.x == 0) mine += sm.kept;
+        mine += numeric_row<W, ITEMS, false, true>(J, item_row(pc.item), sm, vals, err, &pc);
     }
-    if (threadIdx.x == 0 && mine) atomicAdd(&stats->nz_total, mine);
+    if (mine) atomicAdd(&stats->nz_total, mine);
 }
 
 // Scratch layout of the split rows (upper-bound mode): counters | pieces |

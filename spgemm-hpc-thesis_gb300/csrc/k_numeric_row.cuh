@@ -136,7 +136,6 @@ struct RowSmem {
     uint32_t cnt[W * ITEMS];    // kept entries per (warp, item)
     uint16_t seqs[kCap];        // sequence numbers of the unpacked path
     int32_t red[2 * W];         // min / max column reduction
-    uint32_t kept;              // stored entries of the row (upper-bound mode)
     uint32_t step_cnt[64];      // kept counts of one filtered enumeration step (row pieces)
 };
 
@@ -279,8 +278,9 @@ __device__ __forceinline__ void bump16_runs(uint32_t* a, uint32_t i, bool valid,
 }
 
 // Exclusive scan of v over the W*32 threads of a row's team in thread order,
-// with the total and the team-wide maximum of m (red: 2*W words; two barriers
-// for a CTA, none for a warp).
+// with the total and the team-wide maximum of m (red: 2*W words; one barrier
+// for a CTA, none for a warp).  red is next written after later barriers of
+// the row, so no barrier protects it here.
 template <int W>
 __device__ inline uint32_t block_excl_scan_max(uint32_t v, uint32_t m, int32_t* red, int lane, int warp,
                                                uint32_t& total, uint32_t& mx) {
@@ -304,10 +304,23 @@ __device__ inline uint32_t block_excl_scan_max(uint32_t v, uint32_t m, int32_t* 
         tot += s;
         gm = max(gm, static_cast<uint32_t>(red[W + w]));
     }
-    __syncthreads();
     total = tot;
     mx = gm;
     return base + incl - v;
+}
+
+// Zeroes the bucket sort's coarse counters and the fine counters of a row of P
+// products, which the sort expects to find cleared.  Called before the row's
+// enumeration, whose barriers order it before the sort's first atomics; the
+// previous row's sort ended with barriers, so no warp still reads them.
+template <int W, int ITEMS, bool SV>
+__device__ __forceinline__ void clear_buckets(RowSmem<W, ITEMS, SV>& sm, int P, int tid) {
+    constexpr int kExtra = fine_extra(RowSmem<W, ITEMS, SV>::kCap);
+    static_assert((RowSmem<W, ITEMS, SV>::kCap << kExtra) < 65536, "fine bucket numbers are 16-bit");
+    uint32_t* fc = sm.bk + kBkCoarseWords<W> + kBkInfoWords<W>;
+    const int fwords = ((P << kExtra) + 2) >> 1;
+    for (int i = tid; i < kBkCoarseWords<W>; i += W * 32) sm.bk[i] = 0u;
+    for (int i = tid; i < fwords; i += W * 32) fc[i] = 0u;
 }
 
 // Step 2 of a CTA row without digit passes: the products (columns at
@@ -342,13 +355,10 @@ __device__ bool bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int
     const int cbits = nbits < kCoarseBits<W> ? nbits : kCoarseBits<W>;
     const int sc = nbits - cbits;                             // column bits inside a coarse bucket
     const uint32_t scmask = (1u << sc) - 1u;
-    // 0. clear the coarse counters and enough fine counters for P products
+    // 0. the coarse counters and the fine counters of P products are zero on
+    //    entry (clear_buckets, before the row's enumeration)
     constexpr int kExtra = fine_extra(Sm::kCap);
-    static_assert((Sm::kCap << kExtra) < 65536, "fine bucket numbers are 16-bit");
     const int fwords = ((P << kExtra) + 2) >> 1;  // one counter past the last fine bucket
-    for (int i = tid; i < kBkCoarseWords<W>; i += NT) cc[i] = 0u;
-    for (int i = tid; i < fwords; i += NT) fc[i] = 0u;
-    row_sync<W>();
     // 1. coarse histogram
     uint32_t k[ITEMS], f[ITEMS];
 #pragma unroll
@@ -358,9 +368,10 @@ __device__ bool bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int
         bump16_runs(cc, k[i] >> sc, pos < P, lane);
     }
     row_sync<W>();
-    // 2. fine buckets of every coarse bucket, numbered in coarse order (one
-    //    warp)
-    if (warp == 0) {
+    // 2. fine buckets of every coarse bucket, numbered in coarse order: every
+    //    warp computes the whole table and stores it (the same words with the
+    //    same values), so that only a warp-level barrier precedes its use
+    {
         constexpr int kPer = (1 << kCoarseBits<W>) / 32;  // coarse buckets per lane
         uint32_t fcount[kPer], fbits[kPer], sum = 0;
 #pragma unroll
@@ -378,7 +389,7 @@ __device__ bool bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int
             base += fcount[j];
         }
     }
-    row_sync<W>();
+    __syncwarp();
     // 3. fine histogram
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i) {
@@ -631,9 +642,13 @@ __device__ __forceinline__ void radix_sort_fallback(RowSmem<W, ITEMS, SV>& sm, i
 }
 
 // Steps 2-4 of a row for one key layout (PACKED: (col - cmin) << kSeqBits | seq
-// words; otherwise columns and 16-bit sequence numbers).
+// words; otherwise columns and 16-bit sequence numbers).  Returns the stored
+// entries this thread accounts for (its warp's on lane 0 in upper-bound mode,
+// the row's on thread 0 in exact mode, else 0).  No barrier ends the row: the
+// next row's enumeration passes a barrier before it writes what this phase
+// reads (keys, values, sequence numbers, kept counts).
 template <int W, int ITEMS, bool SV, bool PACKED>
-__device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double* vals, int P, uint32_t cmin,
+__device__ uint32_t finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double* vals, int P, uint32_t cmin,
                            int nbits, int lane, int warp, int tid) {
     using Sm = RowSmem<W, ITEMS, SV>;
     constexpr int kSeqBits = Sm::kSeqBits;
@@ -682,16 +697,10 @@ __device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double*
         kept = warp_sum(kept);
         if (W == 1) {
             if (lane == 0) *out.nz = kept;
-        } else {
-            if (lane == 0) atomicAdd(&sm.kept, kept);
-            __syncthreads();
-            if (tid == 0) {
-                if (out.nz_add) atomicAdd(reinterpret_cast<unsigned long long*>(out.nz), sm.kept);
-                else *out.nz = sm.kept;
-            }
+        } else if (lane == 0 && kept) {  // the row's count was zeroed before its enumeration
+            atomicAdd(reinterpret_cast<unsigned long long*>(out.nz), static_cast<unsigned long long>(kept));
         }
-        row_sync<W>();
-        return;
+        return lane == 0 ? kept : 0u;
     }
 
     // 3. runs of equal columns summed in product order; each run's sum is stored
@@ -740,7 +749,8 @@ __device__ void finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, double*
         }
     }
     if (tid == 0) *out.nz = sm.red[0];
-    row_sync<W>();
+    if constexpr (W == 1) __syncwarp();
+    return tid == 0 ? static_cast<uint32_t>(sm.red[0]) : 0u;
 }
 
 
@@ -757,9 +767,10 @@ struct Piece {
 };
 
 // One row (PIECE = false) or one column range of a row (PIECE = true, CTA
-// rows in upper-bound mode only).
+// rows in upper-bound mode only).  Returns the stored entries this thread
+// accounts for (finish_row).
 template <int W, int ITEMS, bool SV, bool PIECE = false>
-__device__ void numeric_row(const Job& J, int row, RowSmem<W, ITEMS, SV>& sm, double* vals, ErrWord* err,
+__device__ uint32_t numeric_row(const Job& J, int row, RowSmem<W, ITEMS, SV>& sm, double* vals, ErrWord* err,
                             const Piece* pc = nullptr) {
     using Sm = RowSmem<W, ITEMS, SV>;
     constexpr int kSeqBits = Sm::kSeqBits;
@@ -767,7 +778,12 @@ __device__ void numeric_row(const Job& J, int row, RowSmem<W, ITEMS, SV>& sm, do
     const int warp = W == 1 ? 0 : (threadIdx.x >> 5);
     const int tid = W == 1 ? lane : threadIdx.x;
     const int P = static_cast<int>(PIECE ? pc->count : J.ub[row]);
-    if (W > 1 && tid == 0) sm.kept = 0;  // read only after the barriers below
+    if constexpr (W > 1) {
+        // an upper-bound row's warps add their kept counts to its count after the
+        // barriers below (a piece's row count was zeroed by the planner)
+        if (!PIECE && J.holes && tid == 0) J.nz[row] = 0;
+        if constexpr (kBucketRows<W, ITEMS>) clear_buckets(sm, P, tid);
+    }
 
     // 1. products into shared memory
     int32_t lo = INT32_MAX, hi = INT32_MIN;
@@ -809,14 +825,15 @@ __device__ void numeric_row(const Job& J, int row, RowSmem<W, ITEMS, SV>& sm, do
             lo = min(lo, sm.red[w]);
             hi = max(hi, sm.red[W + w]);
         }
+    } else {
+        __syncwarp();  // the enumeration's last batch ends without one
     }
-    row_sync<W>();
     const uint32_t cmin = static_cast<uint32_t>(lo);
     const uint32_t range = P ? static_cast<uint32_t>(hi - lo) : 0u;
     const int nbits = range ? 32 - __clz(range) : 0;
     const RowOut out{J.c_col, J.c_val, J.cnt[row] + (PIECE ? pc->slot_off : 0), J.nz + row, J.holes, PIECE ? 1 : 0};
-    if (nbits + kSeqBits <= 32) finish_row<W, ITEMS, SV, true>(out, sm, vals, P, cmin, nbits, lane, warp, tid);
-    else finish_row<W, ITEMS, SV, false>(out, sm, vals, P, cmin, nbits, lane, warp, tid);
+    if (nbits + kSeqBits <= 32) return finish_row<W, ITEMS, SV, true>(out, sm, vals, P, cmin, nbits, lane, warp, tid);
+    return finish_row<W, ITEMS, SV, false>(out, sm, vals, P, cmin, nbits, lane, warp, tid);
 }
 
 constexpr int kWarpKernelThreads = 256;
@@ -844,8 +861,7 @@ num_warp_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items,
         const int64_t it = items[i];
         const Job& J = jobs[item_job(it)];
         const int row = item_row(it);
-        numeric_row<1, ITEMS, true>(J, row, sm, sm.vals, err);
-        if ((threadIdx.x & 31) == 0) mine += static_cast<unsigned long long>(J.nz[row]);
+        mine += numeric_row<1, ITEMS, true>(J, row, sm, sm.vals, err);
     }
     if ((threadIdx.x & 31) == 0 && mine) atomicAdd(&s_nz, mine);
     __syncthreads();
@@ -865,10 +881,9 @@ num_block_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items
         const int64_t it = items[i];
         const Job& J = jobs[item_job(it)];
         const int row = item_row(it);
-        numeric_row<W, ITEMS, SV>(J, row, sm, vals, err);
-        if (threadIdx.x == 0) mine += static_cast<unsigned long long>(J.nz[row]);
+        mine += numeric_row<W, ITEMS, SV>(J, row, sm, vals, err);
     }
-    if (threadIdx.x == 0 && mine) atomicAdd(&stats->nz_total, mine);
+    if (mine) atomicAdd(&stats->nz_total, mine);
 }
 
 inline int capped(int64_t work, int per_block, int cap) {

@@ -170,7 +170,6 @@ struct RowSegs {
     uint64_t valb[NT];
     double scale[NT];
     uint2 word[CAP / 32];
-    int32_t total;
 };
 
 // team_products for rows of at most CAP products (every row the shared-memory
@@ -180,7 +179,9 @@ struct RowSegs {
 // position plus the starts between that position and the product's) instead of
 // a binary search over the batch's prefix sums.  t & 31 is the lane for every
 // product a thread takes (the team strides by multiples of 32), so the mask bits
-// at or below the product's position are lanemask_le.
+// at or below the product's position are lanemask_le.  The last batch ends
+// without a barrier: the caller's next barrier (or, for a warp, __syncwarp)
+// orders the products' shared-memory stores before their readers.
 template <int NT, int CAP, int U = 4, typename F>
 __device__ inline void team_row_products(const Job& J, int row, RowSegs<NT, CAP>& tab, int64_t* s_warp, int tid,
                                          F&& f) {
@@ -197,14 +198,27 @@ __device__ inline void team_row_products(const Job& J, int row, RowSegs<NT, CAP>
         double sc = 1.0;
         int32_t len = 0;
         if (e < nseg) row_segment(J, row, a0, has_s, e, cp, vp, sc, len);
-        // the start mask is cleared before the scan's barriers and set after them
+        // the start mask is cleared before the scan's barrier and set after it
         for (int w = tid; w < CAP / 32; w += NT) tab.word[w].x = 0u;
         if constexpr (NT == 32) __syncwarp();
-        // low 16 bits: products; high 16 bits: non-empty segments
+        // low 16 bits: products; high 16 bits: non-empty segments.  One barrier:
+        // every warp scans the warp totals itself (s_warp is rewritten only
+        // after the batch's later barriers).
         const uint32_t packed = static_cast<uint32_t>(len) | (len > 0 ? 0x10000u : 0u);
-        uint32_t incl;
-        if constexpr (NT == 32) incl = warp_incl_scan(packed, tid);
-        else incl = block_incl_scan<NT>(packed, s_warp);
+        uint32_t incl = warp_incl_scan(packed, lane);
+        uint32_t total_packed;
+        if constexpr (NT == 32) {
+            total_packed = __shfl_sync(0xffffffffu, incl, 31);
+        } else {
+            constexpr int NW = NT / 32;
+            const int warp = tid >> 5;
+            if (lane == 31) s_warp[warp] = incl;
+            __syncthreads();
+            const uint32_t wt = lane < NW ? static_cast<uint32_t>(s_warp[lane]) : 0u;
+            const uint32_t wincl = warp_incl_scan(wt, lane);
+            incl += __shfl_sync(0xffffffffu, wincl - wt, warp);
+            total_packed = __shfl_sync(0xffffffffu, wincl, NW - 1);
+        }
         if (len > 0) {
             const uint32_t s = (incl & 0xffffu) - static_cast<uint32_t>(len);
             const uint32_t r = (incl >> 16) - 1u;
@@ -214,9 +228,8 @@ __device__ inline void team_row_products(const Job& J, int row, RowSegs<NT, CAP>
             atomicOr(&tab.word[s >> 5].x, 1u << (s & 31u));
             for (uint32_t w = (s + 31u) >> 5; (w << 5) < s + static_cast<uint32_t>(len); ++w) tab.word[w].y = r;
         }
-        if (tid == NT - 1) tab.total = static_cast<int32_t>(incl & 0xffffu);
         team_sync<NT>();
-        const int32_t total = tab.total;
+        const int32_t total = static_cast<int32_t>(total_packed & 0xffffu);
         for (int32_t t0 = tid; t0 < total; t0 += U * NT) {
             int r[U];
 #pragma unroll
@@ -242,7 +255,7 @@ __device__ inline void team_row_products(const Job& J, int row, RowSegs<NT, CAP>
                 if (t0 + u * NT < total) f(seq_base + t0 + u * NT, c[u], b[u], tab.scale[r[u]]);
         }
         seq_base += total;
-        team_sync<NT>();
+        if (e0 + NT < nseg) team_sync<NT>();  // the next batch rewrites the table
     }
 }
 
