@@ -55,13 +55,13 @@ __device__ __forceinline__ int hidx(int d, int w) {
     return W == 1 ? d : d * kHistStride<W> + w;
 }
 
-// Bucket sort of CTA rows (bucket_sort below): 2^kCoarseBits<W> coarse
-// buckets, whose 16-bit counters take kBkCoarseWords<W> words and whose table
-// (first fine bucket, fine bits) kBkInfoWords<W>; then at most one fine
-// counter per product.  (7 coarse bits measured 0.25 ms slower on the
-// power-law product.)
+// Bucket sort (bucket_sort below): 2^kCoarseBits<W> coarse buckets (256 for a
+// CTA row, 32 for a warp row), whose 16-bit counters take kBkCoarseWords<W>
+// words and whose table (first fine bucket, fine bits) kBkInfoWords<W>; then
+// the fine counters.  (7 coarse bits for CTA rows measured 0.25 ms slower on
+// the power-law product.)
 template <int W>
-constexpr int kCoarseBits = 8;
+constexpr int kCoarseBits = W == 1 ? 5 : 8;
 template <int W>
 constexpr int kBkCoarseWords = (1 << kCoarseBits<W>) / 2;
 template <int W>
@@ -70,16 +70,18 @@ constexpr int kBkInfoWords = 1 << kCoarseBits<W>;
 // (at most the bucket's column bits), so P products take at most
 // P << fine_extra(cap) fine counters, plus one past the last; fine bucket
 // numbers stay below 2^16 (they are stored in 16-bit words).  On the power-law
-// product one extra bit measured 1.1% faster than none (buckets of 0.5-1
-// products on average instead of 1-2: shorter rank loops), two 5% slower.
+// product one extra bit for CTA rows measured 1.1% faster than none (buckets
+// of 0.5-1 products on average instead of 1-2: shorter rank loops), two 5%
+// slower; for warp rows one extra bit measured 4% slower than none.
 constexpr int kFineExtraBits = 1;
-constexpr int fine_extra(int cap) {
-    int e = kFineExtraBits;
+constexpr int kWarpFineExtraBits = 0;
+constexpr int fine_extra(int cap, int w = 2) {
+    int e = w == 1 ? kWarpFineExtraBits : kFineExtraBits;
     while (e > 0 && (cap << e) >= 65536) --e;
     return e;
 }
 template <int W, int ITEMS>
-constexpr int kBkWords = kBkCoarseWords<W> + kBkInfoWords<W> + ((W * 32 * ITEMS) << fine_extra(W * 32 * ITEMS)) / 2 + 1;
+constexpr int kBkWords = kBkCoarseWords<W> + kBkInfoWords<W> + ((W * 32 * ITEMS) << fine_extra(W * 32 * ITEMS, W)) / 2 + 1;
 
 // In the packed layout the scatter also stores every product's fine bucket
 // beside it (in the sequence-number array, which that layout leaves unused),
@@ -100,12 +102,18 @@ constexpr int rank_group(int items) {
         if (items % g == 0) return g;
     return 1;
 }
-// Which rows take the bucket sort: CTA rows.  Warp rows keep the radix sort,
-// whose passes need no barrier across warps; the bucket sort for warp rows of
-// 3-12 products per lane (32 coarse buckets) measured 0.1 ms slower on the
-// power-law product and 2% slower on the uniform one.
+// Which rows take the bucket sort: CTA rows, and warp rows of 8-16 products per
+// lane (32 coarse buckets, no extra fine bit, so that a warp's counters stay
+// small).  On the power-law product, with the bins on three streams, K4 took
+// 12.64 -> 12.10 ms, uniform 0.204 -> 0.199 ms; on one stream the 512-product
+// bin alone is slower (0.77 -> 0.94 ms: a warp row's passes need no barrier,
+// so the radix sort's extra instructions cost little while the bin runs
+// alone), but beside the CTA bins the fewer instructions win.  Warp rows of 6
+// products per lane measured the same either way; fewer keep the radix sort.
+constexpr int kWarpBucketMinItems = 8;
+constexpr int kWarpBucketMaxItems = 16;
 template <int W, int ITEMS>
-constexpr bool kBucketRows = W > 1;
+constexpr bool kBucketRows = W > 1 || (ITEMS >= kWarpBucketMinItems && ITEMS <= kWarpBucketMaxItems);
 // A fine bucket holding more products than this (a column repeated many times)
 // sends the row to the radix sort: ranking inside a bucket is quadratic.
 constexpr uint32_t kMaxFine = 64;
@@ -315,7 +323,7 @@ __device__ inline uint32_t block_excl_scan_max(uint32_t v, uint32_t m, int32_t* 
 // previous row's sort ended with barriers, so no warp still reads them.
 template <int W, int ITEMS, bool SV>
 __device__ __forceinline__ void clear_buckets(RowSmem<W, ITEMS, SV>& sm, int P, int tid) {
-    constexpr int kExtra = fine_extra(RowSmem<W, ITEMS, SV>::kCap);
+    constexpr int kExtra = fine_extra(RowSmem<W, ITEMS, SV>::kCap, W);
     static_assert((RowSmem<W, ITEMS, SV>::kCap << kExtra) < 65536, "fine bucket numbers are 16-bit");
     uint32_t* fc = sm.bk + kBkCoarseWords<W> + kBkInfoWords<W>;
     const int fwords = ((P << kExtra) + 2) >> 1;
@@ -357,7 +365,7 @@ __device__ bool bucket_sort(RowSmem<W, ITEMS, SV>& sm, int P, uint32_t cmin, int
     const uint32_t scmask = (1u << sc) - 1u;
     // 0. the coarse counters and the fine counters of P products are zero on
     //    entry (clear_buckets, before the row's enumeration)
-    constexpr int kExtra = fine_extra(Sm::kCap);
+    constexpr int kExtra = fine_extra(Sm::kCap, W);
     const int fwords = ((P << kExtra) + 2) >> 1;  // one counter past the last fine bucket
     // 1. coarse histogram
     uint32_t k[ITEMS], f[ITEMS];
@@ -637,7 +645,7 @@ __device__ __forceinline__ void radix_sort_fallback(RowSmem<W, ITEMS, SV>& sm, i
     radix_sort_row<W, ITEMS, SV, false, false>(sm, P, cmin, nbits, lane, warp, tid);
     if constexpr (PACKED) {
         for (int i = tid; i < P; i += W * 32) sm.keys[i] = ((sm.keys[i] - cmin) << kSeqBits) | sm.seqs[i];
-        __syncthreads();
+        row_sync<W>();  // a warp row's team is its warp: never a CTA barrier there
     }
 }
 
@@ -782,8 +790,8 @@ __device__ uint32_t numeric_row(const Job& J, int row, RowSmem<W, ITEMS, SV>& sm
         // an upper-bound row's warps add their kept counts to its count after the
         // barriers below (a piece's row count was zeroed by the planner)
         if (!PIECE && J.holes && tid == 0) J.nz[row] = 0;
-        if constexpr (kBucketRows<W, ITEMS>) clear_buckets(sm, P, tid);
     }
+    if constexpr (kBucketRows<W, ITEMS>) clear_buckets(sm, P, tid);
 
     // 1. products into shared memory
     int32_t lo = INT32_MAX, hi = INT32_MIN;

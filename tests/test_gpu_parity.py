@@ -76,6 +76,29 @@ def column_window_case(width: int, seed: int):
     return a, b
 
 
+def test_repeated_columns_next_to_wide_rows(engine, port):
+    # Rows whose products fall on three columns (a column repeated more than 64
+    # times makes the bucket sort hand the row to the radix sort) interleaved
+    # with rows of wide column ranges, in every bin from 100 to 6,000 products:
+    # in one launch some teams of a kernel take the radix fallback and others do
+    # not, which must not disturb one another's results or the stored count.
+    rng = np.random.default_rng(11)
+    nb = 2000
+    b_cols = np.where(np.arange(nb)[:, None] < nb // 2, rng.integers(0, 3, size=(nb, 16)),
+                      rng.integers(0, 3000, size=(nb, 16))).astype(np.int32)
+    b = Csr(nb, 3000, np.arange(0, 16 * nb + 1, 16, dtype=np.int64), b_cols.ravel(),
+            rng.uniform(-1, 1, size=16 * nb))
+    rows = []
+    for t in (100, 200, 240, 300, 450, 700, 1000, 1500, 3000, 6000):
+        for r in range(64):
+            lo = 0 if r % 2 == 0 else nb // 2
+            rows.append(rng.integers(lo, lo + nb // 2, size=t // 16))
+    rp = np.zeros(len(rows) + 1, dtype=np.int64)
+    rp[1:] = np.cumsum([len(x) for x in rows])
+    a = Csr(len(rows), nb, rp, np.concatenate(rows).astype(np.int32), rng.uniform(-1, 1, size=int(rp[-1])))
+    check(engine, port, a, b)
+
+
 @pytest.mark.parametrize("width", [0, 1, 3, 4, 5, 8, 9, 12, 13, 16, 17, 19, 20, 21, 24, 25])
 def test_column_range_widths(engine, port, width):
     # The radix sort takes 8-bit passes and a last pass of at most 4 bits, over
