@@ -293,7 +293,7 @@ template <int W>
 __device__ inline uint32_t block_excl_scan_max(uint32_t v, uint32_t m, int32_t* red, int lane, int warp,
                                                uint32_t& total, uint32_t& mx) {
     const uint32_t incl = warp_incl_scan(v, lane);
-    const uint32_t wm = warp_max(m);
+    const uint32_t wm = __reduce_max_sync(0xffffffffu, m);
     if constexpr (W == 1) {
         total = __shfl_sync(0xffffffffu, incl, 31);
         mx = wm;
@@ -702,7 +702,7 @@ __device__ uint32_t finish_row(const RowOut& out, RowSmem<W, ITEMS, SV>& sm, dou
                 if (oc >= 0) out.c_val[out0 + pos] = acc;
             }
         }
-        kept = warp_sum(kept);
+        kept = __reduce_add_sync(0xffffffffu, kept);
         if (W == 1) {
             if (lane == 0) *out.nz = kept;
         } else if (lane == 0 && kept) {  // the row's count was zeroed before its enumeration
@@ -818,8 +818,8 @@ __device__ uint32_t numeric_row(const Job& J, int row, RowSmem<W, ITEMS, SV>& sm
                                             [&](int32_t seq, int32_t c, double b, double a) {
                                                 put(seq, c, __dmul_rn(a, b));
                                             });
-    lo = warp_min(lo);
-    hi = warp_max(hi);
+    lo = __reduce_min_sync(0xffffffffu, lo);  // one warp-wide reduction instruction each
+    hi = __reduce_max_sync(0xffffffffu, hi);
     if (W > 1) {
         if (lane == 0) {
             sm.red[warp] = lo;
