@@ -369,18 +369,26 @@ split_plan_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ item
 template <int W, int ITEMS, int MINB>
 __global__ void __launch_bounds__(W * 32, MINB)
 num_piece_kernel(const Job* __restrict__ jobs, SplitPlan plan, Stats* __restrict__ stats, ErrWord* __restrict__ err,
-                 double* __restrict__ gvals) {
+                 double* __restrict__ gvals, unsigned long long* __restrict__ ticket) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ RowQueue q;  // pieces from the launch's queue, as the row kernels take rows
     using Sm = RowSmem<W, ITEMS, false>;
     Sm& sm = *reinterpret_cast<Sm*>(smem_raw);
     double* vals = gvals + static_cast<size_t>(blockIdx.x) * Sm::kCap;
     const int64_t count = min(static_cast<int64_t>(*plan.counters), plan.max_pieces);
     unsigned long long mine = 0;
-    for (int64_t i = blockIdx.x; i < count; i += gridDim.x) {
+    int par = 0;
+    for (int64_t i = blockIdx.x; i < count; par ^= 1) {
+        if (threadIdx.x == 0)
+            q.next[par] = static_cast<int64_t>(gridDim.x) + static_cast<int64_t>(atomicAdd(ticket, 1ull));
         const Piece pc = plan.pieces[i];
-        if (pc.count <= 0) continue;  // an empty last piece (same for the whole CTA)
-        const Job& J = jobs[item_job(pc.item)];
-        mine += numeric_row<W, ITEMS, false, true>(J, item_row(pc.item), sm, vals, err, &pc);
+        if (pc.count > 0) {
+            const Job& J = jobs[item_job(pc.item)];
+            mine += numeric_row<W, ITEMS, false, true>(J, item_row(pc.item), sm, vals, err, &pc);
+        } else {
+            __syncthreads();  // an empty last piece (same for the whole CTA): no row barrier orders the queue
+        }
+        i = q.next[par];
     }
     if (mine) atomicAdd(&stats->nz_total, mine);
 }
@@ -504,7 +512,7 @@ static double* tail_slab(void* d_scratch, size_t scratch_bytes, size_t need) {
 
 // Rows of more than kSplitThreshold products in upper-bound mode: plan and
 // stage, the pieces, then the rows left to the global-slab sort.
-static void launch_split(const Job* d_jobs, const int64_t* d_items, int64_t count, int64_t max_ub,
+static void launch_split(int bin, const Job* d_jobs, const int64_t* d_items, int64_t count, int64_t max_ub,
                          const SplitTotals& split, void* d_scratch, Stats* d_stats, ErrWord* d_err, cudaStream_t st,
                          int num_sms) {
     const SplitLayout L = split_layout(max_ub, split, num_sms);
@@ -525,7 +533,9 @@ static void launch_split(const Job* d_jobs, const int64_t* d_items, int64_t coun
     const int smem = static_cast<int>(sizeof(PieceSm));
     auto kern = num_piece_kernel<kPieceW, kPieceItems, kPieceMinB>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    kern<<<num_sms * kPieceMinB, kPieceW * 32, smem, st>>>(d_jobs, plan, d_stats, d_err, static_cast<double*>(slabs));
+    // the bin's own queue: bins 17-19 each plan and run their pieces, one after the other
+    kern<<<num_sms * kPieceMinB, kPieceW * 32, smem, st>>>(d_jobs, plan, d_stats, d_err, static_cast<double*>(slabs),
+                                                          &d_stats->ticket[bin]);
     num_heavy_kernel<<<heavy_grid(count, num_sms), kHeavyThreads, 0, st>>>(
         d_jobs, plan.fallback, count, slabs, max_ub, d_stats, d_err, plan.counters + 1);
 }
@@ -545,39 +555,40 @@ void launch_numeric(int bin, const Job* d_jobs, const int64_t* d_items, int64_t 
     // does -- the autotuner keeps it where it measures faster.
     const bool whole = variant == 1 && bin < kBinHeavy;
     if (holes && bin > kLastSmemBin && !whole) {
-        launch_split(d_jobs, d_items, count, max_ub, split, d_scratch, d_stats, d_err, st, num_sms);
+        launch_split(bin, d_jobs, d_items, count, max_ub, split, d_scratch, d_stats, d_err, st, num_sms);
         return;
     }
     double* slab = static_cast<double*>(d_scratch);
+    unsigned long long* const tk = &d_stats->ticket[bin];  // the bin's row queue
     switch (bin) {
-        case 9: run_block<4, 6, 8>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;     // <= 768
+        case 9: run_block<4, 6, 8>(d_jobs, d_items, count, d_stats, d_err, st, num_sms, tk); break;     // <= 768
         case 10:  // <= 1024
-            run_block<kB10W, kB10I, kB10MinB, kB10SV>(d_jobs, d_items, count, d_stats, d_err, st, num_sms,
+            run_block<kB10W, kB10I, kB10MinB, kB10SV>(d_jobs, d_items, count, d_stats, d_err, st, num_sms, tk,
                                                      tail_slab(d_scratch, scratch_bytes, cta_slab_bytes(10, count, num_sms)));
             break;
         case 11:  // <= 1536
-            run_block<kB11W, kB11I, kB11MinB, kB11SV>(d_jobs, d_items, count, d_stats, d_err, st, num_sms,
+            run_block<kB11W, kB11I, kB11MinB, kB11SV>(d_jobs, d_items, count, d_stats, d_err, st, num_sms, tk,
                                                      tail_slab(d_scratch, scratch_bytes, cta_slab_bytes(11, count, num_sms)));
             break;
-        case 12: run_block<8, 8, 4>(d_jobs, d_items, count, d_stats, d_err, st, num_sms); break;    // <= 2048
+        case 12: run_block<8, 8, 4>(d_jobs, d_items, count, d_stats, d_err, st, num_sms, tk); break;    // <= 2048
         case 13:  // <= 3072
-            run_block<kB13W, kB13I, kB13MinB, kB13SV>(d_jobs, d_items, count, d_stats, d_err, st, num_sms,
+            run_block<kB13W, kB13I, kB13MinB, kB13SV>(d_jobs, d_items, count, d_stats, d_err, st, num_sms, tk,
                                                      tail_slab(d_scratch, scratch_bytes, cta_slab_bytes(13, count, num_sms)));
             break;
         case 14:  // <= 4096
-            run_block<kB14W, kB14I, kB14MinB, kB14SV>(d_jobs, d_items, count, d_stats, d_err, st, num_sms,
+            run_block<kB14W, kB14I, kB14MinB, kB14SV>(d_jobs, d_items, count, d_stats, d_err, st, num_sms, tk,
                                                      tail_slab(d_scratch, scratch_bytes, cta_slab_bytes(14, count, num_sms)));
             break;
         case 15:  // <= 6144
-            run_block<kB15W, kB15I, kB15MinB, kB15SV>(d_jobs, d_items, count, d_stats, d_err, st, num_sms,
+            run_block<kB15W, kB15I, kB15MinB, kB15SV>(d_jobs, d_items, count, d_stats, d_err, st, num_sms, tk,
                                                      tail_slab(d_scratch, scratch_bytes, cta_slab_bytes(15, count, num_sms)));
             break;
         case 16:  // <= 8192
-            run_block<kB16W, kB16I, kB16MinB, kB16SV>(d_jobs, d_items, count, d_stats, d_err, st, num_sms,
+            run_block<kB16W, kB16I, kB16MinB, kB16SV>(d_jobs, d_items, count, d_stats, d_err, st, num_sms, tk,
                                                      tail_slab(d_scratch, scratch_bytes, cta_slab_bytes(16, count, num_sms)));
             break;
-        case 17: run_block<16, 24, 1, false>(d_jobs, d_items, count, d_stats, d_err, st, num_sms, slab); break;
-        case 18: run_block<16, 32, 1, false>(d_jobs, d_items, count, d_stats, d_err, st, num_sms, slab); break;
+        case 17: run_block<16, 24, 1, false>(d_jobs, d_items, count, d_stats, d_err, st, num_sms, tk, slab); break;
+        case 18: run_block<16, 32, 1, false>(d_jobs, d_items, count, d_stats, d_err, st, num_sms, tk, slab); break;
         case kBinHeavy:  // exact layout (the upper-bound layout splits these rows)
             num_heavy_kernel<<<heavy_grid(count, num_sms), kHeavyThreads, 0, st>>>(
                 d_jobs, d_items, count, d_scratch, max_ub, d_stats, d_err, nullptr);

@@ -112,6 +112,9 @@ struct Stats {
     unsigned long long sym_total;     // sum of cnt
     unsigned long long nz_total;      // sum of nz
     unsigned long long split_products;  // sum of ub over rows of more than kSplitThreshold products
+    // the row queue of each bin's numeric launch: rows (or, for the split rows
+    // of bins 17-19, pieces) handed out past the launch's first wave
+    unsigned long long ticket[kNumBins];
 };
 
 // The rows of more than kSplitThreshold products of a call: their scalar
