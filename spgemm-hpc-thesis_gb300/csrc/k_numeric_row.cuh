@@ -27,6 +27,8 @@
 // (num_heavy_kernel, k_numeric.cu).
 #pragma once
 
+#include <atomic>
+
 #include <type_traits>
 
 #include "spg_enum.cuh"
@@ -940,7 +942,19 @@ void run_block(const Job* jobs, const int64_t* items, int64_t count, Stats* stat
                int num_sms, unsigned long long* ticket, double* gvals = nullptr) {
     const int smem = static_cast<int>(sizeof(RowSmem<W, ITEMS, SV>));
     cudaFuncSetAttribute(num_block_kernel<W, ITEMS, MINB, SV>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    const int grid = SV ? capped(count, 1, num_sms * (MINB > 8 ? MINB : 8)) : slab_grid(count, num_sms, MINB);
+    // One wave of resident CTAs: with the row queue, CTAs beyond it would start
+    // only once the queue has run dry (slab bins: one slab per resident CTA).
+    static std::atomic<int> resident{0};  // per instantiation (every device of this build is an sm_103a)
+    int nb = resident.load(std::memory_order_relaxed);
+    if (nb == 0) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, num_block_kernel<W, ITEMS, MINB, SV>, W * 32, smem) !=
+                cudaSuccess || nb < 1) {
+            cudaGetLastError();
+            nb = MINB;
+        }
+        resident.store(nb, std::memory_order_relaxed);
+    }
+    const int grid = SV ? capped(count, 1, num_sms * nb) : slab_grid(count, num_sms, MINB);
     num_block_kernel<W, ITEMS, MINB, SV><<<grid, W * 32, smem, st>>>(jobs, items, count, stats, err, gvals, ticket);
 }
 
