@@ -176,8 +176,11 @@ spg_status spg_last_timings(const spg_handle* handle, spg_timings* timings);
  * split into column-range pieces: at 8,192 (default) or at 16,384, the rows in
  * between then running whole, one 16-warp CTA each.  Results are identical,
  * times differ with the workload.  spg_tune multiplies A * B reps times (after one warm-up) with every
- * bin on its default shape, then on its alternative, and keeps, per bin, the
- * alternative where its median numeric time was at least 3% lower.  The choice
+ * bin on its default shape, then on its alternative, the bins one after the
+ * other; a bin whose alternative's median numeric time was at least 3% lower is
+ * a candidate, which is then kept only if, with the bins on their streams as
+ * calls run them, the median numeric phase with it is at least 0.5% shorter
+ * than without it (2 x (reps + 1) more multiplies per candidate).  The choice
  * stays on the handle for later multiplies, batches, to-host products and plans
  * (spg_get/set_bin_variants save and restore it: 20 entries of 0 or 1). */
 typedef struct {

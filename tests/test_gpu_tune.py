@@ -40,10 +40,26 @@ def test_tune_keeps_results(engine, port):
         assert rep["products"] == engine.scalar_multiplication_count(a, a)
         for name, v in rep["bins"].items():
             assert v["ms_default"] > 0 and v["ms_alt"] > 0
+            # a kept alternative was a candidate: at least 3% faster with the bins one after the other
+            assert not v["variant"] or v["ms_alt"] < 0.97 * v["ms_default"], (name, v)
         after = engine.multiply(a, a)
         assert csr_bits_equal(after, before), explain_diff(after, before)
     finally:
         engine.bin_variants = [0] * 20
+
+
+def test_tune_on_one_stream_keeps_results():
+    # bins on one stream: the candidates are kept without the confirmation pass
+    from spgemm_gb300 import Engine
+    a = synth_powerlaw(20000, 24.0, 1.2, 3000, 256, 0.7, seed=8)
+    with Engine(0, bin_streams=1) as eng:
+        before = eng.multiply(a, a)
+        rep = eng.tune(a, a, reps=1)
+        assert eng.bin_variants == rep["variants"]
+        for name, v in rep["bins"].items():
+            assert not v["variant"] or v["ms_alt"] < 0.97 * v["ms_default"], (name, v)
+        after = eng.multiply(a, a)
+        assert csr_bits_equal(after, before), explain_diff(after, before)
 
 
 def test_set_bin_variants_rejects_bad_values(engine):
