@@ -886,7 +886,8 @@ num_warp_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items,
 // launch's row queue: the CTA's first row is its index, each later one
 // gridDim.x plus the next ticket of the bin's counter, so that rows of very
 // different cost spread over the CTAs as they free up.  Thread 0 fetches the
-// ticket at the start of the current row (its latency hides behind the row)
+// ticket at the start of the current row (the other warps start on the row
+// meanwhile; fetching it a row ahead instead, in a register, measured slower)
 // into one of two shared words (alternating rows); every thread reads it after
 // the row, whose barriers order the store before the reads, and every read
 // before the store two rows later.
@@ -907,7 +908,8 @@ num_block_kernel(const Job* __restrict__ jobs, const int64_t* __restrict__ items
     unsigned long long mine = 0;
     int par = 0;
     for (int64_t i = blockIdx.x; i < count; par ^= 1) {
-        if (threadIdx.x == 0) q.next[par] = static_cast<int64_t>(gridDim.x) + static_cast<int64_t>(atomicAdd(ticket, 1ull));
+        if (threadIdx.x == 0)
+            q.next[par] = static_cast<int64_t>(gridDim.x) + static_cast<int64_t>(atomicAdd(ticket, 1ull));
         const int64_t it = items[i];
         const Job& J = jobs[item_job(it)];
         const int row = item_row(it);
